@@ -1,0 +1,399 @@
+#!/usr/bin/env python
+"""Throughput of DualAveragingStepSizeAdaptation(NoUTurnSampler) on GB300.
+
+Workload (default, ``nuts_logreg_1e5x100``): Bayesian logistic regression,
+X [100000, 100] float32 with column 0 = 1 and the other columns iid
+N(0, 1)/sqrt(100), true beta ~ N(0, I), y ~ Bernoulli(sigmoid(X beta)),
+prior N(0, I); 1024 chains initialised N(0, 0.1^2); NUTS max_tree_depth=10
+inside dual averaging (target accept 0.8, 1000 adaptation steps, initial
+step 0.1).  Seeded synthetic data (numpy default_rng(1)).
+
+A step is one transition of the whole 1024-chain batch.  ``value`` is useful
+gradient evaluations per second (sum over chains of NUTS leapfrogs_taken,
+the reference's accounting, nuts.py:433-435) over the K timed steps with the
+chain state resident in HBM.  ``e2e`` repeats K steps through the public
+API with the state, log-density and gradients copied in from pinned host
+memory and the next state and accept ratios copied back every step.
+
+``--impl reference`` times the CPU restatement of the reference algorithm
+(the oracle, NumPy float32, all host threads) on the same workload.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+WORKLOADS = {
+    'nuts_logreg_1e5x100': dict(n=100000, d=100, chains=1024, depth=10, seed=1,
+                                feature_scale=0.1, step0=0.1, target_accept=0.8,
+                                num_adaptation_steps=1000, precision='fp32'),
+}
+METRIC = 'grad-evals/s (NUTS leapfrogs_taken summed over chains; min-ESS/s reported beside)'
+
+
+def make_data(w):
+  rng = np.random.default_rng(w['seed'])
+  X = rng.normal(size=(w['n'], w['d'])) * w['feature_scale']
+  X[:, 0] = 1.0
+  beta = rng.normal(size=w['d'])
+  p = 1.0 / (1.0 + np.exp(-(X @ beta)))
+  y = (rng.uniform(size=w['n']) < p).astype(np.float32)
+  init = (rng.normal(size=(w['chains'], w['d'])) * 0.1).astype(np.float32)
+  return X.astype(np.float32), y, init
+
+
+class ClockSampler:
+  """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+  FIELDS = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+            'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+            'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+  def __init__(self, gpu_index):
+    self.gpu = gpu_index
+    self.proc = None
+    self.lines = []
+
+  def start(self):
+    try:
+      self.proc = subprocess.Popen(
+          ['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.FIELDS,
+           '--format=csv,noheader,nounits', '-lms', '200'],
+          stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+      self.thread = threading.Thread(target=self._read, daemon=True)
+      self.thread.start()
+    except (OSError, ValueError):
+      self.proc = None
+
+  def _read(self):
+    for line in self.proc.stdout:
+      self.lines.append(line.strip())
+
+  def stop(self):
+    if self.proc is None:
+      return None
+    self.proc.terminate()
+    try:
+      self.proc.wait(timeout=5)
+    except subprocess.TimeoutExpired:
+      self.proc.kill()
+    sm, mx, reasons = [], None, set()
+    names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+    for ln in self.lines:
+      parts = [p.strip() for p in ln.split(',')]
+      if len(parts) < 9:
+        continue
+      try:
+        sm.append(float(parts[1]))
+        mx = float(parts[2])
+      except ValueError:
+        continue
+      for nm, v in zip(names, parts[5:9]):
+        if v.lower() == 'active':
+          reasons.add(nm)
+    if not sm:
+      return None
+    return {'sm_mhz': statistics.median(sm), 'sm_max_mhz': mx, 'reasons': sorted(reasons),
+            'samples': len(sm)}
+
+
+def read_peaks():
+  try:
+    return json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json'))), 'measured'
+  except (OSError, ValueError):
+    return {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0, 'bf16_tflops_sustained': 1700.0}, 'fallback'
+
+
+def read_traffic(kernel_name):
+  """Per-launch DRAM traffic of the dominant kernel from the committed ncu
+  summary (profiles/traffic.json), if one was captured for this kernel."""
+  try:
+    t = json.load(open(os.path.join(ROOT, 'profiles', 'traffic.json')))
+    return t.get(kernel_name)
+  except (OSError, ValueError):
+    return None
+
+
+def dist_setup(args):
+  world = int(os.environ.get('WORLD_SIZE', '1'))
+  rank = int(os.environ.get('RANK', '0'))
+  local = int(os.environ.get('LOCAL_RANK', '0'))
+  return world, rank, local
+
+
+def cpu_baseline_run(w, X, y, init, max_seconds, steps_cap, state=None, step_size=None):
+  """Time the oracle (CPU restatement, float32, all host threads)."""
+  from oracle import mcmc as omcmc
+  from oracle import philox
+  from oracle import targets as ot
+
+  Xf = X.astype(np.float32)
+  yf = y.astype(np.float32)
+
+  def target(q):
+    q = q.astype(np.float32)
+    z = q @ Xf.T
+    lp = -(np.logaddexp(0, z) * (1 - yf) + np.logaddexp(0, -z) * yf).sum(-1, dtype=np.float64)
+    lp += (-0.5 * q.astype(np.float64) ** 2 - 0.5 * np.log(2 * np.pi)).sum(-1)
+    r = yf - 1.0 / (1.0 + np.exp(-z))
+    return lp, (r @ Xf - q).astype(np.float32)
+
+  q = init.copy() if state is None else state.copy()
+  lp, g = target(q)
+  da = omcmc.DualAveraging(w['step0'] if step_size is None else step_size,
+                           w['num_adaptation_steps'], w['target_accept'])
+  evals, steps = 0, 0
+  t0 = time.perf_counter()
+  while steps < steps_cap:
+    r = omcmc.nuts_one_step(target, q, lp, g, np.float32(da.new_step_size),
+                            philox.PhiloxDraws(philox.step_key((w['seed'], 0), steps)),
+                            w['depth'], dtype=np.float32)
+    q, lp, g = r.next_state, r.target_log_prob, r.grads_target_log_prob
+    da.update(r.log_accept_ratio)
+    evals += int(r.leapfrogs_taken.sum())
+    steps += 1
+    if time.perf_counter() - t0 > max_seconds:
+      break
+  dt = time.perf_counter() - t0
+  return evals / dt, steps, dt
+
+
+def run_reference(args, w):
+  world, rank, _ = dist_setup(args)
+  if rank != 0:
+    return
+  X, y, init = make_data(w)
+  budget = float(os.environ.get('GBM_REFERENCE_SECONDS', '150'))
+  rate, steps, dt = cpu_baseline_run(w, X, y, init, budget, args.steps + args.warmup)
+  cores = os.cpu_count()
+  line = {
+      'impl': 'reference', 'metric': METRIC, 'value': rate, 'unit': 'grad-evals/s',
+      'n_gpus': args.gpus, 'steps': steps, 'warmup': 0, 'ms_per_step': 1000 * dt / max(steps, 1),
+      'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+      'data': 'synthetic (seeded numpy)',
+      'config': {'workload': args.workload, 'chains': w['chains'], 'rows': w['n'],
+                 'features': w['d'], 'max_tree_depth': w['depth'], 'parallelism': 'replicas'},
+      'cpu_baseline': {'value': rate, 'unit': 'grad-evals/s', 'cores': cores, 'kind': 'port',
+                       'sample': '%d DA(NUTS) transitions of all %d chains from the initial '
+                                 'state, NumPy float32 oracle, BLAS threads = %d, stopped after '
+                                 '%.0f s' % (steps, w['chains'], cores, budget)},
+      'e2e': {'value': rate, 'unit': 'grad-evals/s', 'h2d_bytes_per_step': 0,
+              'd2h_bytes_per_step': 0},
+  }
+  print(json.dumps(line), flush=True)
+
+
+def run_engine(args, w):
+  import torch
+  world, rank, local = dist_setup(args)
+  torch.cuda.set_device(local)
+  dist = None
+  if world > 1:
+    import torch.distributed as dist
+    dist.init_process_group('nccl')
+  import probability_gb300 as pg
+  from probability_gb300 import _native
+
+  X, y, init = make_data(w)
+  if world > 1:  # independent replicas: per-rank init state
+    init = (np.random.default_rng(w['seed'] + 100 * rank).normal(size=init.shape) * 0.1
+            ).astype(np.float32)
+  target = pg.LogisticRegression(X, y, precision=args.precision or w['precision'])
+  nuts = pg.mcmc.NoUTurnSampler(target, step_size=w['step0'], max_tree_depth=w['depth'])
+  kernel = pg.mcmc.DualAveragingStepSizeAdaptation(
+      nuts, num_adaptation_steps=w['num_adaptation_steps'],
+      target_accept_prob=w['target_accept'])
+  dev = torch.device('cuda', local)
+  state = torch.from_numpy(init).to(dev)
+  kr = kernel.bootstrap_results(state)
+  seed = (w['seed'], rank)
+  t = 0
+
+  def step(state, kr, t):
+    return kernel.one_step(state, kr, seed=pg._util.step_key(seed, t))
+
+  for _ in range(args.warm_in + args.warmup):       # adaptation warm-in + warmup
+    state, kr = step(state, kr, t)
+    t += 1
+  torch.cuda.synchronize()
+  l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+  def barrier():
+    if dist is not None:
+      dist.barrier()
+    torch.cuda.synchronize()
+
+  # ---- device-resident timed region ----
+  _native.check(_native.lib().gbm_nuts_set_profiling(nuts._handle, 1))
+  import ctypes
+  ms0, ev0, la0 = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+  _native.lib().gbm_nuts_read_profile(nuts._handle, ctypes.byref(ms0), ctypes.byref(ev0),
+                                      ctypes.byref(la0))
+  clocks = ClockSampler(local)
+  clocks.start()
+  lf_total = torch.zeros((), dtype=torch.int64, device=dev)
+  draws = []
+  step_ms = 0.0
+  barrier()
+  wall0 = time.perf_counter()
+  for _ in range(args.steps):
+    l2_flush.zero_()                                  # L2 flush outside the events
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    state, kr = step(state, kr, t)
+    e1.record()
+    t += 1
+    lf_total += kr.inner_results.leapfrogs_taken.sum()
+    draws.append(state)
+    e1.synchronize()
+    step_ms += e0.elapsed_time(e1)
+  barrier()
+  wall = time.perf_counter() - wall0
+  clk = clocks.stop()
+  eval_ms, evals, launches = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+  _native.check(_native.lib().gbm_nuts_read_profile(
+      nuts._handle, ctypes.byref(eval_ms), ctypes.byref(evals), ctypes.byref(launches)))
+  _native.lib().gbm_nuts_set_profiling(nuts._handle, 0)
+  grad_evals = int(lf_total.item())
+  secs = step_ms / 1000.0
+  if dist is not None:
+    tt = torch.tensor([secs], device=dev)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    secs = float(tt.item())
+    ge = torch.tensor([grad_evals], device=dev, dtype=torch.int64)
+    dist.all_reduce(ge)
+    grad_evals = int(ge.item())
+  value = grad_evals / secs
+  draws_t = torch.stack(draws)
+  ess = pg.mcmc.effective_sample_size(draws_t, filter_beyond_positive_pairs=True).sum(0)
+  min_ess_per_s = float(ess.min().item()) / secs if args.steps >= 8 else None
+
+  # ---- roofline of the dominant kernel (batched gradient) ----
+  flops_per_grad, bytes_per_batch = target.cost(1)
+  alg_flops = flops_per_grad * (grad_evals if dist is None else int(lf_total.item()))
+  peaks, peak_src = read_peaks()
+  eval_s = eval_ms.value / 1000.0
+  achieved_tflops = alg_flops / eval_s / 1e12 if eval_s > 0 else None
+  tensor_peak = peaks['bf16_tflops']
+  kernel_name = 'logreg_partial_kernel' if target.precision == 'fp32' else 'logreg_tc_kernel'
+  roofline = {
+      'bound': 'tensor', 'achieved': achieved_tflops, 'peak': tensor_peak, 'unit': 'TFLOP/s',
+      'frac': achieved_tflops / tensor_peak if achieved_tflops else None,
+      'traffic': read_traffic(kernel_name), 'kernel': kernel_name,
+      'peak_source': peak_src + ' (MEASURED_PEAKS.json bf16_tflops burst)',
+      'eval_launches': int(evals.value), 'eval_ms_total': eval_ms.value,
+      'alg_flops_per_grad_eval': flops_per_grad,
+  }
+  if target.precision == 'fp32':
+    roofline['note'] = ('FP32 CUDA-core kernel (plain FP32 form); the roof shown is the BF16 '
+                        'tensor-core peak, so frac understates its use of the FP32 pipes')
+
+  # ---- end-to-end through host buffers ----
+  C, D = state.shape
+  h_state = torch.empty((C, D), dtype=torch.float32).pin_memory()
+  h_tlp = torch.empty(C, dtype=torch.float64).pin_memory()
+  h_grad = torch.empty((C, D), dtype=torch.float32).pin_memory()
+  h_out = torch.empty((C, D), dtype=torch.float32).pin_memory()
+  h_lar = torch.empty(C, dtype=torch.float64).pin_memory()
+  h_state.copy_(state.cpu())
+  h_tlp.copy_(kr.inner_results.target_log_prob.cpu())
+  h_grad.copy_(kr.inner_results.grads_target_log_prob.cpu())
+  e2e_steps = max(1, args.steps)
+  lf_e2e = torch.zeros((), dtype=torch.int64, device=dev)
+  barrier()
+  e0 = torch.cuda.Event(enable_timing=True)
+  e1 = torch.cuda.Event(enable_timing=True)
+  e0.record()
+  for _ in range(e2e_steps):
+    d_state = h_state.to(dev, non_blocking=True)
+    inner = kr.inner_results._replace(
+        target_log_prob=h_tlp.to(dev, non_blocking=True),
+        grads_target_log_prob=h_grad.to(dev, non_blocking=True))
+    kr = kr._replace(inner_results=inner)
+    state, kr = step(d_state, kr, t)
+    t += 1
+    lf_e2e += kr.inner_results.leapfrogs_taken.sum()
+    h_out.copy_(state, non_blocking=True)
+    h_lar.copy_(kr.inner_results.log_accept_ratio, non_blocking=True)
+    h_tlp.copy_(kr.inner_results.target_log_prob, non_blocking=True)
+    h_grad.copy_(kr.inner_results.grads_target_log_prob, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    h_state.copy_(h_out)
+  e1.record()
+  e1.synchronize()
+  e2e_s = e0.elapsed_time(e1) / 1000.0
+  e2e_value = int(lf_e2e.item()) / e2e_s
+  h2d = C * D * 4 * 2 + C * 8
+  d2h = C * D * 4 * 2 + C * 8 * 2
+
+  cpu = None
+  if rank == 0 and world == 1 and not args.no_cpu_baseline:
+    budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '20'))
+    rate, nsteps, dt = cpu_baseline_run(w, X, y, init, budget, 1000000,
+                                        state=state.cpu().numpy(),
+                                        step_size=float(kr.new_step_size.reshape(-1)[0].item()))
+    cpu = {'value': rate, 'unit': 'grad-evals/s', 'cores': os.cpu_count(), 'kind': 'port',
+           'sample': '%d DA(NUTS) transitions of all %d chains from the engine\'s adapted '
+                     'state (%.1f s), NumPy float32 oracle, BLAS threads = all cores'
+                     % (nsteps, w['chains'], dt)}
+
+  if rank == 0:
+    line = {
+        'metric': METRIC, 'value': value, 'unit': 'grad-evals/s', 'n_gpus': world,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': step_ms / args.steps,
+        'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32' if target.precision == 'fp32' else 'bf16+f32',
+        'data': 'synthetic (seeded numpy default_rng(%d))' % w['seed'],
+        'config': {'workload': args.workload, 'rows': w['n'], 'features': w['d'],
+                   'chains': w['chains'], 'max_tree_depth': w['depth'],
+                   'target_accept_prob': w['target_accept'],
+                   'num_adaptation_steps': w['num_adaptation_steps'],
+                   'precision': target.precision, 'warm_in_transitions': args.warm_in,
+                   'l2': 'flushed between timed steps (256 MB write outside the step events)',
+                   'parallelism': 'replicas' if world > 1 else 'single'},
+        'min_ess_per_s': min_ess_per_s,
+        'step_size': float(kr.new_step_size.reshape(-1)[0].item()),
+        'mean_leapfrogs_per_chain_step': grad_evals / (args.steps * w['chains'] * world),
+        'wall_s_timed_region': wall,
+        'e2e': {'value': e2e_value, 'unit': 'grad-evals/s', 'h2d_bytes_per_step': h2d,
+                'd2h_bytes_per_step': d2h, 'steps': e2e_steps},
+        'roofline': roofline,
+        'cpu_baseline': cpu,
+        'gpu_launches': int(launches.value) + args.steps,
+        'clocks': clk,
+    }
+    print(json.dumps(line), flush=True)
+  if dist is not None:
+    dist.destroy_process_group()
+
+
+def main():
+  ap = argparse.ArgumentParser()
+  ap.add_argument('--gpus', type=int, default=1)
+  ap.add_argument('--steps', type=int, default=30)
+  ap.add_argument('--warmup', type=int, default=5)
+  ap.add_argument('--warm-in', type=int, default=100,
+                  help='untimed dual-averaging transitions before warmup')
+  ap.add_argument('--impl', default='engine', choices=['engine', 'reference'])
+  ap.add_argument('--workload', default='nuts_logreg_1e5x100', choices=sorted(WORKLOADS))
+  ap.add_argument('--precision', default=None, choices=[None, 'fp32', 'mixed'])
+  ap.add_argument('--no-cpu-baseline', action='store_true')
+  args = ap.parse_args()
+  w = WORKLOADS[args.workload]
+  if args.impl == 'reference':
+    run_reference(args, w)
+  else:
+    run_engine(args, w)
+
+
+if __name__ == '__main__':
+  main()

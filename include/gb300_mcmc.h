@@ -1,0 +1,175 @@
+/*
+ * gb300_mcmc.h -- C ABI of the GB300 (sm_103a) gradient-MCMC engine.
+ *
+ * Plain C: opaque handles, raw device pointers and sizes.  Every function
+ * returns an int status (GBM_OK == 0); on failure gbm_last_error() returns a
+ * thread-local message.  Numerical trouble (NaN/inf log-densities, divergent
+ * trajectories) is never an error: it is reported in-band exactly as the
+ * reference does (rejection, -inf log-accept ratios, divergence flags).
+ *
+ * Layouts: states are chain-major float32 [chains][dim] (the reference's
+ * [C, D] batch layout, mcmc/hmc.py:184-192); log-densities, energies and
+ * log-accept ratios are float64 [chains]; flags are uint8 [chains].
+ * All tensor pointers are device pointers on the context's device; calls are
+ * asynchronous on the context's stream unless stated otherwise.
+ *
+ * Reference paths are relative to tensorflow_probability/python/.
+ */
+#ifndef GB300_MCMC_H_
+#define GB300_MCMC_H_
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define GBM_API __attribute__((visibility("default")))
+#else
+#define GBM_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBM_OK 0
+#define GBM_EINVAL 22
+#define GBM_ENOMEM 12
+#define GBM_ENOTSUP 95
+#define GBM_ETIMEDOUT 110
+#define GBM_ECUDA 1000
+
+#define GBM_DTYPE_F32 0
+#define GBM_DTYPE_BF16 1
+
+/* Precision of a target's contractions.  F32: CUDA-core FP32 ("plain FP32").
+ * MIXED: BF16 tensor-core contractions with FP32 accumulation and a
+ * hi/lo split of the FP32 operands (residual correction). */
+#define GBM_PRECISION_F32 0
+#define GBM_PRECISION_MIXED 1
+
+typedef struct gbm_context gbm_context;
+typedef struct gbm_target gbm_target;
+typedef struct gbm_hmc gbm_hmc;
+typedef struct gbm_nuts gbm_nuts;
+
+/* Library version (major * 10000 + minor * 100 + patch). */
+GBM_API int gbm_version(void);
+
+/* Message of the last failed call on this thread ("" if none). */
+GBM_API const char* gbm_last_error(void);
+
+/* Execution context: one device, one stream.  cuda_stream is the caller's
+ * cudaStream_t (NULL = the device's default stream); every call of this
+ * context is ordered on it.  There is no reference counterpart (TFP runs
+ * on TensorFlow's device context, mcmc/nuts_test.py:516). */
+GBM_API int gbm_context_create(int device, void* cuda_stream, gbm_context** out);
+GBM_API int gbm_context_destroy(gbm_context* ctx);
+GBM_API int gbm_context_synchronize(gbm_context* ctx);
+
+/* Key of transition `step` in sample_chain's seed stream: the first two words
+ * of Philox4x32-10(seed; step, STEP_KEY).  Replaces the reference's per-step
+ * samplers.split_seed (mcmc/sample.py:344-349) with an addressable stream.
+ * Host-only, no device work. */
+GBM_API int gbm_step_key(const uint32_t seed[2], uint64_t step, uint32_t out[2]);
+
+/* ---- target_log_prob_fn families ------------------------------------ */
+
+/* Bayesian logistic regression: X [num_rows][num_features] (row-major,
+ * dtype x_dtype), y [num_rows] float32 in {0,1}, iid Normal(0, prior_scale)
+ * prior.  Replaces the user's target_log_prob_fn + autodiff
+ * (mcmc/internal/util.py:286-308, math/gradient.py:28) for the
+ * inference_gym logistic-regression target
+ * (spinoffs/inference_gym/inference_gym/targets/logistic_regression.py:92-103,
+ * distributions/bernoulli.py:126-140).  X and y are copied. */
+GBM_API int gbm_target_logistic_regression(gbm_context* ctx, const void* x, int x_dtype,
+                                   int64_t num_rows, int64_t num_features, const float* y,
+                                   float prior_scale, int precision, gbm_target** out);
+GBM_API int gbm_target_destroy(gbm_target* target);
+GBM_API int gbm_target_dim(const gbm_target* target, int64_t* dim);
+
+/* Batched log-density and gradient at `chains` states (the value-and-gradient
+ * call of mcmc/internal/util.py:246-283).  log_prob: float64 [chains];
+ * grad: float32 [chains][dim]. */
+GBM_API int gbm_target_log_prob_and_grad(gbm_target* target, const float* state, int64_t chains,
+                                 double* log_prob, float* grad);
+
+/* Algorithmic flops and HBM bytes of one batched evaluation at `chains`. */
+GBM_API int gbm_target_cost(const gbm_target* target, int64_t chains, double* flops, double* bytes);
+
+/* ---- HamiltonianMonteCarlo ------------------------------------------- */
+
+/* One transition of MetropolisHastings(UncalibratedHamiltonianMonteCarlo)
+ * (mcmc/hmc.py:501-529 -> mcmc/metropolis_hastings.py:160-254,
+ * mcmc/hmc.py:661-729).  step_size: float32 device scalar, or [chains] when
+ * step_size_per_chain != 0.  seed: 2 x uint32 host words keying the
+ * momentum and MH-uniform draws.  Any of the optional outputs
+ * (proposed_*, initial_momentum, final_momentum, log_acceptance_correction)
+ * may be NULL. */
+GBM_API int gbm_hmc_create(gbm_target* target, int64_t max_chains, gbm_hmc** out);
+GBM_API int gbm_hmc_destroy(gbm_hmc* kernel);
+GBM_API int gbm_hmc_one_step(gbm_hmc* kernel, int64_t chains, const float* state,
+                     const double* target_log_prob, const float* grads_target_log_prob,
+                     const float* step_size, int step_size_per_chain,
+                     int32_t num_leapfrog_steps, const uint32_t seed[2],
+                     float* next_state, double* next_target_log_prob,
+                     float* next_grads_target_log_prob, float* proposed_state,
+                     double* proposed_target_log_prob, float* proposed_grads_target_log_prob,
+                     float* initial_momentum, float* final_momentum,
+                     double* log_acceptance_correction, double* log_accept_ratio,
+                     uint8_t* is_accepted);
+
+/* ---- NoUTurnSampler -------------------------------------------------- */
+
+/* NoUTurnSampler(target, step_size, max_tree_depth, max_energy_diff,
+ * unrolled_leapfrog_steps) (mcmc/nuts.py:197-275).  Allocates the
+ * per-chain trajectory workspace for up to max_chains chains. */
+GBM_API int gbm_nuts_create(gbm_target* target, int64_t max_chains, int32_t max_tree_depth,
+                    double max_energy_diff, int32_t unrolled_leapfrog_steps, gbm_nuts** out);
+GBM_API int gbm_nuts_destroy(gbm_nuts* kernel);
+
+/* NoUTurnSampler.one_step (mcmc/nuts.py:321-445).  Outputs are the fields of
+ * NUTSKernelResults (nuts.py:74-91) plus the next state; tree_depth may be
+ * NULL.  Blocks the host at most once per tree depth to read whether any
+ * chain continues (the reference's tf.while_loop condition, nuts.py:404-407). */
+GBM_API int gbm_nuts_one_step(gbm_nuts* kernel, int64_t chains, const float* state,
+                      const double* target_log_prob, const float* grads_target_log_prob,
+                      const float* step_size, int step_size_per_chain, const uint32_t seed[2],
+                      float* next_state, double* next_target_log_prob,
+                      float* next_grads_target_log_prob, double* log_accept_ratio,
+                      int32_t* leapfrogs_taken, uint8_t* is_accepted, uint8_t* reach_max_depth,
+                      uint8_t* has_divergence, double* energy, int32_t* tree_depth);
+
+/* Number of leaf iterations (batched gradient evaluations) the last
+ * gbm_nuts_one_step launched. */
+GBM_API int gbm_nuts_last_leaf_iterations(const gbm_nuts* kernel, int64_t* out);
+
+/* Profiling of NUTS transitions.  When enabled, CUDA events on the context
+ * stream bracket every batched target evaluation.  gbm_nuts_read_profile
+ * synchronizes the stream and returns, since the previous read, the summed
+ * device time of those evaluations (ms), their count, and the number of
+ * kernels this handle launched (targets' kernels included), then resets. */
+GBM_API int gbm_nuts_set_profiling(gbm_nuts* kernel, int enable);
+GBM_API int gbm_nuts_read_profile(gbm_nuts* kernel, double* eval_ms, int64_t* evals,
+                                  int64_t* kernel_launches);
+
+/* ---- DualAveragingStepSizeAdaptation ----------------------------------- */
+
+/* One dual-averaging update after an inner one_step
+ * (mcmc/dual_averaging_step_size_adaptation.py:353-475, 477-532).
+ * log_accept_ratio: float64 [chains] from the inner kernel.
+ * state: float64 [groups][4] = (error_sum, log_averaging_step,
+ * log_shrinkage_target, step) with groups = 1 (shared step size, chains
+ * reduced by reduce_logmeanexp) or chains (per-chain step sizes).
+ * step_size: float32 [groups]; on entry the step size used by this
+ * transition, on exit the next one (new_step_size).  target_accept_prob:
+ * float64 [groups] device array, or NULL to use `target_accept_scalar`. */
+GBM_API int gbm_dual_averaging_update(gbm_context* ctx, int64_t chains, const double* log_accept_ratio,
+                              int per_chain, int32_t num_adaptation_steps,
+                              double target_accept_scalar, const double* target_accept_prob,
+                              double exploration_shrinkage, double step_count_smoothing,
+                              double decay_rate, double* state, float* step_size);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif  /* GB300_MCMC_H_ */

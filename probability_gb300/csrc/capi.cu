@@ -1,0 +1,369 @@
+// C-ABI entry points (include/gb300_mcmc.h): argument checks, error
+// reporting, handle lifetime.  All numerical work is in the kernels of
+// logreg_*.cu and samplers.cu.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <new>
+#include <string>
+
+#include "gb300_mcmc.h"
+#include "rng.cuh"
+#include "samplers.h"
+
+namespace gbm {
+
+static thread_local std::string g_last_error;
+
+void set_error(const std::string& msg) { g_last_error = msg; }
+
+std::unique_ptr<Target> make_logreg_tc(gbm_context* ctx, const void* X, int x_dtype, int64_t n,
+                                       int64_t d, const float* y, float prior_scale);
+
+}  // namespace gbm
+
+using gbm::set_error;
+
+namespace {
+
+template <class F>
+int guarded(F&& f) {
+  try {
+    return f();
+  } catch (const gbm::CudaError& e) {
+    set_error(std::string(e.what) + ": " + cudaGetErrorString(e.err));
+    return e.err == cudaErrorMemoryAllocation ? GBM_ENOMEM : GBM_ECUDA;
+  } catch (const std::bad_alloc&) {
+    set_error("host allocation failed");
+    return GBM_ENOMEM;
+  } catch (const std::exception& e) {
+    set_error(e.what());
+    return GBM_EINVAL;
+  }
+}
+
+int invalid(const std::string& msg) {
+  set_error(msg);
+  return GBM_EINVAL;
+}
+
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    cudaGetDevice(&prev);
+    if (prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    cudaGetDevice(&cur);
+    if (prev >= 0 && cur != prev) cudaSetDevice(prev);
+  }
+};
+
+}  // namespace
+
+extern "C" {
+
+int gbm_version(void) { return 100; }
+
+const char* gbm_last_error(void) { return gbm::g_last_error.c_str(); }
+
+int gbm_step_key(const uint32_t seed[2], uint64_t step, uint32_t out[2]) {
+  if (!seed || !out) return invalid("gbm_step_key: NULL argument");
+  if (step >= ((uint64_t)1 << 32)) return invalid("gbm_step_key: step must be < 2^32");
+  const uint2 k = gbm::step_key(make_uint2(seed[0], seed[1]), (uint32_t)step);
+  out[0] = k.x;
+  out[1] = k.y;
+  return GBM_OK;
+}
+
+int gbm_context_create(int device, void* stream, gbm_context** out) {
+  if (!out) return invalid("gbm_context_create: out is NULL");
+  return guarded([&] {
+    int n = 0;
+    GBM_CUDA(cudaGetDeviceCount(&n));
+    if (device < 0 || device >= n) return invalid("gbm_context_create: bad device index");
+    DeviceGuard g(device);
+    auto* ctx = new gbm_context();
+    ctx->device = device;
+    ctx->stream = static_cast<cudaStream_t>(stream);   // NULL: the default stream
+    ctx->owns_stream = false;
+    GBM_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+    ctx->host_flag_slots = 16;
+    GBM_CUDA(cudaMallocHost(&ctx->host_flags, sizeof(int) * ctx->host_flag_slots));
+    *out = ctx;
+    return GBM_OK;
+  });
+}
+
+int gbm_context_destroy(gbm_context* ctx) {
+  if (!ctx) return GBM_OK;
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    if (ctx->host_flags) cudaFreeHost(ctx->host_flags);
+    if (ctx->owns_stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GBM_OK;
+  });
+}
+
+int gbm_context_synchronize(gbm_context* ctx) {
+  if (!ctx) return invalid("gbm_context_synchronize: ctx is NULL");
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    GBM_CUDA(cudaStreamSynchronize(ctx->stream));
+    return GBM_OK;
+  });
+}
+
+int gbm_target_logistic_regression(gbm_context* ctx, const void* x, int x_dtype,
+                                   int64_t num_rows, int64_t num_features, const float* y,
+                                   float prior_scale, int precision, gbm_target** out) {
+  if (!ctx || !x || !y || !out) return invalid("gbm_target_logistic_regression: NULL argument");
+  if (num_rows <= 0 || num_features <= 0)
+    return invalid("gbm_target_logistic_regression: num_rows and num_features must be > 0");
+  if (num_rows > (int64_t)1 << 31)
+    return invalid("gbm_target_logistic_regression: num_rows must be < 2^31");
+  if (!(prior_scale > 0.f))
+    return invalid("gbm_target_logistic_regression: prior_scale must be > 0");
+  if (x_dtype != GBM_DTYPE_F32 && x_dtype != GBM_DTYPE_BF16)
+    return invalid("gbm_target_logistic_regression: x_dtype must be GBM_DTYPE_F32 or BF16");
+  if (precision != GBM_PRECISION_F32 && precision != GBM_PRECISION_MIXED)
+    return invalid("gbm_target_logistic_regression: unknown precision");
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    auto* t = new gbm_target();
+    t->ctx = ctx;
+    if (precision == GBM_PRECISION_F32) {
+      if (x_dtype != GBM_DTYPE_F32) {
+        delete t;
+        return invalid("gbm_target_logistic_regression: FP32 precision needs float32 X");
+      }
+      t->impl = gbm::make_logreg_simt(ctx, static_cast<const float*>(x), num_rows, num_features,
+                                      y, prior_scale);
+      if (!t->impl) {
+        delete t;
+        return invalid("gbm_target_logistic_regression: FP32 path supports num_features <= 256");
+      }
+    } else {
+      t->impl = gbm::make_logreg_tc(ctx, x, x_dtype, num_rows, num_features, y, prior_scale);
+      if (!t->impl) {
+        delete t;
+        set_error("gbm_target_logistic_regression: mixed-precision path unavailable for this shape");
+        return GBM_ENOTSUP;
+      }
+    }
+    GBM_CUDA(cudaMalloc(&t->count.ptr, sizeof(int)));
+    t->count.bytes = sizeof(int);
+    GBM_CUDA(cudaStreamSynchronize(ctx->stream));
+    *out = t;
+    return GBM_OK;
+  });
+}
+
+int gbm_target_destroy(gbm_target* t) {
+  if (!t) return GBM_OK;
+  return guarded([&] {
+    DeviceGuard g(t->ctx->device);
+    cudaStreamSynchronize(t->ctx->stream);
+    delete t;
+    return GBM_OK;
+  });
+}
+
+int gbm_target_dim(const gbm_target* t, int64_t* dim) {
+  if (!t || !dim) return invalid("gbm_target_dim: NULL argument");
+  *dim = t->impl->dim;
+  return GBM_OK;
+}
+
+int gbm_target_cost(const gbm_target* t, int64_t chains, double* flops, double* bytes) {
+  if (!t || !flops || !bytes) return invalid("gbm_target_cost: NULL argument");
+  *flops = t->impl->flops(chains);
+  *bytes = t->impl->bytes(chains);
+  return GBM_OK;
+}
+
+int gbm_target_log_prob_and_grad(gbm_target* t, const float* state, int64_t chains,
+                                 double* log_prob, float* grad) {
+  if (!t || !state || !log_prob || !grad) return invalid("gbm_target_log_prob_and_grad: NULL argument");
+  if (chains <= 0 || chains > (1 << 24)) return invalid("gbm_target_log_prob_and_grad: bad chains");
+  return guarded([&] {
+    DeviceGuard g(t->ctx->device);
+    cudaStream_t s = t->ctx->stream;
+    t->ws.reserve(t->impl->workspace_bytes(chains));
+    const int n = (int)chains;
+    GBM_CUDA(cudaMemcpyAsync(t->count.ptr, &n, sizeof(int), cudaMemcpyHostToDevice, s));
+    t->impl->eval(state, (int)t->impl->dim, t->count.as<int>(), n, log_prob, grad,
+                  (int)t->impl->dim, t->ws.ptr, s);
+    // The count word is host memory of this frame; finish the copy before
+    // returning.
+    GBM_CUDA(cudaStreamSynchronize(s));
+    return GBM_OK;
+  });
+}
+
+int gbm_hmc_create(gbm_target* target, int64_t max_chains, gbm_hmc** out) {
+  if (!target || !out) return invalid("gbm_hmc_create: NULL argument");
+  if (max_chains <= 0 || max_chains > (1 << 24)) return invalid("gbm_hmc_create: bad max_chains");
+  return guarded([&] {
+    DeviceGuard g(target->ctx->device);
+    auto* k = new gbm_hmc();
+    k->target = target;
+    k->max_chains = max_chains;
+    try {
+      gbm::hmc_setup(k);
+    } catch (...) {
+      delete k;
+      throw;
+    }
+    *out = k;
+    return GBM_OK;
+  });
+}
+
+int gbm_hmc_destroy(gbm_hmc* k) {
+  if (!k) return GBM_OK;
+  return guarded([&] {
+    DeviceGuard g(k->target->ctx->device);
+    cudaStreamSynchronize(k->target->ctx->stream);
+    delete k;
+    return GBM_OK;
+  });
+}
+
+int gbm_hmc_one_step(gbm_hmc* k, int64_t chains, const float* state,
+                     const double* target_log_prob, const float* grads,
+                     const float* step_size, int step_size_per_chain,
+                     int32_t num_leapfrog_steps, const uint32_t seed[2],
+                     float* next_state, double* next_tlp, float* next_grads,
+                     float* proposed_state, double* proposed_tlp, float* proposed_grads,
+                     float* initial_momentum, float* final_momentum,
+                     double* log_acceptance_correction, double* log_accept_ratio,
+                     uint8_t* is_accepted) {
+  if (!k || !state || !target_log_prob || !grads || !step_size || !seed || !next_state ||
+      !next_tlp || !next_grads || !log_accept_ratio || !is_accepted)
+    return invalid("gbm_hmc_one_step: NULL argument");
+  if (chains <= 0 || chains > k->max_chains)
+    return invalid("gbm_hmc_one_step: chains must be in [1, max_chains]");
+  if (num_leapfrog_steps < 1) return invalid("gbm_hmc_one_step: num_leapfrog_steps must be >= 1");
+  return guarded([&] {
+    DeviceGuard g(k->target->ctx->device);
+    gbm::HmcOutputs out{next_state, next_tlp, next_grads, proposed_state, proposed_tlp,
+                        proposed_grads, initial_momentum, final_momentum,
+                        log_acceptance_correction, log_accept_ratio, is_accepted};
+    gbm::hmc_one_step(k, chains, state, target_log_prob, grads, step_size, step_size_per_chain,
+                      num_leapfrog_steps, make_uint2(seed[0], seed[1]), out);
+    return GBM_OK;
+  });
+}
+
+int gbm_nuts_create(gbm_target* target, int64_t max_chains, int32_t max_tree_depth,
+                    double max_energy_diff, int32_t unrolled_leapfrog_steps, gbm_nuts** out) {
+  if (!target || !out) return invalid("gbm_nuts_create: NULL argument");
+  if (max_tree_depth < 1 || max_tree_depth > 16)
+    return invalid("max_tree_depth must be known statically and >= 1 (engine limit 16)");
+  if (max_chains <= 0 || max_chains > (1 << 24)) return invalid("gbm_nuts_create: bad max_chains");
+  if (unrolled_leapfrog_steps < 1) return invalid("gbm_nuts_create: unrolled_leapfrog_steps < 1");
+  return guarded([&] {
+    DeviceGuard g(target->ctx->device);
+    auto* k = new gbm_nuts();
+    k->target = target;
+    k->max_chains = max_chains;
+    k->max_tree_depth = max_tree_depth;
+    k->max_energy_diff = max_energy_diff;
+    k->unrolled_leapfrog_steps = unrolled_leapfrog_steps;
+    try {
+      gbm::nuts_setup(k);
+    } catch (...) {
+      delete k;
+      throw;
+    }
+    *out = k;
+    return GBM_OK;
+  });
+}
+
+int gbm_nuts_destroy(gbm_nuts* k) {
+  if (!k) return GBM_OK;
+  return guarded([&] {
+    DeviceGuard g(k->target->ctx->device);
+    cudaStreamSynchronize(k->target->ctx->stream);
+    for (auto& ev : k->poll_events)
+      if (ev) cudaEventDestroy(ev);
+    for (auto& ev : k->prof_events) cudaEventDestroy(ev);
+    delete k;
+    return GBM_OK;
+  });
+}
+
+int gbm_nuts_one_step(gbm_nuts* k, int64_t chains, const float* state,
+                      const double* target_log_prob, const float* grads,
+                      const float* step_size, int step_size_per_chain, const uint32_t seed[2],
+                      float* next_state, double* next_tlp, float* next_grads,
+                      double* log_accept_ratio, int32_t* leapfrogs_taken, uint8_t* is_accepted,
+                      uint8_t* reach_max_depth, uint8_t* has_divergence, double* energy,
+                      int32_t* tree_depth) {
+  if (!k || !state || !target_log_prob || !grads || !step_size || !seed || !next_state ||
+      !next_tlp || !next_grads || !log_accept_ratio || !leapfrogs_taken || !is_accepted ||
+      !reach_max_depth || !has_divergence || !energy)
+    return invalid("gbm_nuts_one_step: NULL argument");
+  if (chains <= 0 || chains > k->max_chains)
+    return invalid("gbm_nuts_one_step: chains must be in [1, max_chains]");
+  return guarded([&] {
+    DeviceGuard g(k->target->ctx->device);
+    gbm::NutsOutputs out{next_state, next_tlp, next_grads, log_accept_ratio, leapfrogs_taken,
+                         is_accepted, reach_max_depth, has_divergence, energy, tree_depth};
+    gbm::nuts_one_step(k, chains, state, target_log_prob, grads, step_size, step_size_per_chain,
+                       make_uint2(seed[0], seed[1]), out);
+    return GBM_OK;
+  });
+}
+
+int gbm_nuts_last_leaf_iterations(const gbm_nuts* k, int64_t* out) {
+  if (!k || !out) return invalid("gbm_nuts_last_leaf_iterations: NULL argument");
+  *out = k->last_leaf_iterations;
+  return GBM_OK;
+}
+
+int gbm_nuts_set_profiling(gbm_nuts* k, int enable) {
+  if (!k) return invalid("gbm_nuts_set_profiling: NULL argument");
+  k->profiling = enable != 0;
+  return GBM_OK;
+}
+
+int gbm_nuts_read_profile(gbm_nuts* k, double* eval_ms, int64_t* evals, int64_t* launches) {
+  if (!k || !eval_ms || !evals || !launches) return invalid("gbm_nuts_read_profile: NULL argument");
+  return guarded([&] {
+    DeviceGuard g(k->target->ctx->device);
+    GBM_CUDA(cudaStreamSynchronize(k->target->ctx->stream));
+    gbm::nuts_profile_flush(k);
+    *eval_ms = k->prof_eval_ms;
+    *evals = k->prof_evals;
+    *launches = k->prof_launches;
+    k->prof_eval_ms = 0.0;
+    k->prof_evals = 0;
+    k->prof_launches = 0;
+    return GBM_OK;
+  });
+}
+
+int gbm_dual_averaging_update(gbm_context* ctx, int64_t chains, const double* lar, int per_chain,
+                              int32_t num_adaptation_steps, double target_accept_scalar,
+                              const double* target_accept_prob, double exploration_shrinkage,
+                              double step_count_smoothing, double decay_rate, double* state,
+                              float* step_size) {
+  if (!ctx || !lar || !state || !step_size) return invalid("gbm_dual_averaging_update: NULL argument");
+  if (chains <= 0) return invalid("gbm_dual_averaging_update: chains must be > 0");
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    gbm::DaParams prm{target_accept_scalar, exploration_shrinkage, step_count_smoothing,
+                      decay_rate, num_adaptation_steps};
+    gbm::dual_averaging_update(ctx->stream, lar, chains, per_chain, prm, target_accept_prob,
+                               state, step_size);
+    return GBM_OK;
+  });
+}
+
+}  // extern "C"

@@ -1,0 +1,71 @@
+// Internal C++ interfaces of the engine (not part of the C-ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <memory>
+#include <vector>
+
+#include "common.cuh"
+
+struct gbm_context {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool owns_stream = false;
+  int num_sms = 0;
+  // Pinned host words the host polls for NUTS loop control.
+  int* host_flags = nullptr;
+  int host_flag_slots = 0;
+};
+
+namespace gbm {
+
+// Device memory owned by a handle; freed on destruction.
+struct DeviceBuffer {
+  void* ptr = nullptr;
+  size_t bytes = 0;
+  DeviceBuffer() = default;
+  DeviceBuffer(const DeviceBuffer&) = delete;
+  DeviceBuffer& operator=(const DeviceBuffer&) = delete;
+  ~DeviceBuffer() { if (ptr) cudaFree(ptr); }
+  void reserve(size_t b) {
+    if (b <= bytes) return;
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+    if (b == 0) return;
+    GBM_CUDA(cudaMalloc(&ptr, b));
+    bytes = b;
+  }
+  template <class T> T* as() const { return static_cast<T*>(ptr); }
+};
+
+// A built-in model family: batched log-density + gradient over a dense batch.
+// Rows 0..n-1 of `q` (row stride ldq floats) are states; n is read on the
+// device from *n_dev (so samplers can compact active chains without a host
+// round trip) and never exceeds `cap`.  Outputs: logp[n] (float64),
+// grad[n][ldg] (float32).  `ws` is scratch of workspace_bytes(cap).
+struct Target {
+  virtual ~Target() = default;
+  int64_t dim = 0;
+  virtual size_t workspace_bytes(int64_t cap) const = 0;
+  virtual void eval(const float* q, int ldq, const int* n_dev, int cap, double* logp,
+                    float* grad, int ldg, void* ws, cudaStream_t s) = 0;
+  // Algorithmic flops and HBM bytes for one batched evaluation of n states.
+  virtual double flops(int64_t n) const = 0;
+  virtual double bytes(int64_t n) const = 0;
+  // Kernels one eval() launches (for launch accounting).
+  virtual int launches_per_eval() const = 0;
+};
+
+std::unique_ptr<Target> make_logreg_simt(gbm_context* ctx, const float* X, int64_t n,
+                                         int64_t d, const float* y, float prior_scale);
+
+}  // namespace gbm
+
+struct gbm_target {
+  gbm_context* ctx = nullptr;
+  std::unique_ptr<gbm::Target> impl;
+  gbm::DeviceBuffer ws;       // eval scratch
+  gbm::DeviceBuffer count;    // one int: batch size for direct calls
+};

@@ -1,0 +1,283 @@
+// Fused logistic-regression log-density + gradient, FP32 CUDA cores.
+//
+// For a dense batch of n chain states B[n][D] and data X[N][D], y[N]:
+//   z      = X B^T                           (N x n)
+//   logp_c = sum_r [-softplus(z) (1-y) - softplus(-z) y] + log N(B_c; 0, s)
+//   R      = y - sigmoid(z)
+//   grad_c = X^T R_c - B_c / s^2
+// which is what the reference obtains by autodiff of the inference_gym
+// logistic-regression target (spinoffs/inference_gym/inference_gym/targets/
+// logistic_regression.py:92-103 with distributions/bernoulli.py:126-140).
+//
+// One CTA owns a (chain tile of 64, row split) work item.  Per 64-row tile of
+// X it computes Z = X_tile B_tile^T (register-tiled 4x4 per thread), the
+// log-likelihood and R in the epilogue (R goes to shared memory only), then
+// G += R^T X_tile with G held in registers across the CTA's rows: X is read
+// from HBM/L2 once per chain tile and Z/R never leave the SM.  Each CTA
+// writes one partial (logp, G); a second kernel sums the partials in fixed
+// split order (deterministic) and adds the prior.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <memory>
+
+#include "engine.h"
+
+namespace gbm {
+namespace {
+
+constexpr int kCT = 64;        // chains per tile
+constexpr int kNT = 64;        // data rows per tile
+constexpr int kThreads = 256;
+constexpr int kXPad = kNT + 4;  // Xt row stride (floats)
+
+__host__ __device__ inline int num_splits(int n, int grid, int row_tiles) {
+  const int tiles = (n + kCT - 1) / kCT;
+  if (tiles == 0) return 0;
+  int s = grid / tiles;
+  s = s < 1 ? 1 : s;
+  return s > row_tiles ? row_tiles : s;
+}
+
+__device__ __forceinline__ float sigmoidf_(float z) { return 1.f / (1.f + expf(-z)); }
+
+template <int KD>
+__global__ void __launch_bounds__(kThreads)
+logreg_partial_kernel(const float* __restrict__ X, int ldx, const float* __restrict__ y, int N,
+                      int D, const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev,
+                      int grid, double* __restrict__ lpart, float* __restrict__ gpart) {
+  extern __shared__ __align__(16) float smem[];
+  const int n = *n_dev;
+  const int row_tiles = (N + kNT - 1) / kNT;
+  const int S = num_splits(n, grid, row_tiles);
+  const int tiles = (n + kCT - 1) / kCT;
+  const int item = blockIdx.x;
+  if (S == 0 || item >= tiles * S) return;
+  const int tile = item % tiles, split = item / tiles;
+  const int c0 = tile * kCT;
+  const int rt_begin = (int)((long long)split * row_tiles / S);
+  const int rt_end = (int)((long long)(split + 1) * row_tiles / S);
+  const int Dp = KD * 16;  // padded feature count held in shared memory
+
+  float* Bt = smem;                    // [Dp][kCT]
+  float* Xt = Bt + Dp * kCT;           // [Dp][kXPad]
+  float* Rs = Xt + Dp * kXPad;         // [kNT][kCT]
+  __shared__ double red[kThreads / 16][16][4];
+
+  const int tid = threadIdx.x;
+  // B tile, transposed: Bt[d][c] = Q[c0 + c][d]; zero outside (n, D).
+  for (int i = tid; i < Dp * kCT; i += kThreads) {
+    const int c = i / Dp, d = i % Dp;
+    float v = 0.f;
+    if (c0 + c < n && d < D) v = Q[(size_t)(c0 + c) * ldq + d];
+    Bt[d * kCT + c] = v;
+  }
+  // Rows of Xt beyond D stay zero for the whole kernel.
+  for (int i = tid; i < (Dp - D) * kXPad; i += kThreads) Xt[D * kXPad + i] = 0.f;
+
+  const int ty = tid >> 4, tx = tid & 15;   // phase 1: rows ty*4.., chains tx*4..
+  const int cg = tid >> 4, dg = tid & 15;   // phase 2: chains cg*4.., d = dg + 16k
+  float g[4][KD];
+#pragma unroll
+  for (int j = 0; j < 4; ++j)
+#pragma unroll
+    for (int k = 0; k < KD; ++k) g[j][k] = 0.f;
+  double lp_acc[4] = {0.0, 0.0, 0.0, 0.0};
+
+  for (int rt = rt_begin; rt < rt_end; ++rt) {
+    const int r0 = rt * kNT;
+    __syncthreads();  // previous tile's phase 2 is done with Xt/Rs
+    // X tile, transposed into Xt[d][r] (coalesced global reads along d).
+    for (int i = tid; i < kNT * D; i += kThreads) {
+      const int r = i / D, d = i % D;
+      const int row = r0 + r;
+      Xt[d * kXPad + r] = row < N ? X[(size_t)row * ldx + d] : 0.f;
+    }
+    __syncthreads();
+    // Phase 1: Z[r][c] = sum_d Xt[d][r] Bt[d][c].
+    float acc[4][4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    for (int d = 0; d < D; ++d) {
+      const float4 xv = *reinterpret_cast<const float4*>(&Xt[d * kXPad + ty * 4]);
+      const float4 bv = *reinterpret_cast<const float4*>(&Bt[d * kCT + tx * 4]);
+      const float xa[4] = {xv.x, xv.y, xv.z, xv.w};
+      const float ba[4] = {bv.x, bv.y, bv.z, bv.w};
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(xa[i], ba[j], acc[i][j]);
+    }
+    // Epilogue: log-likelihood terms and residuals R = y - sigmoid(z).
+    float lp_tile[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int row = r0 + ty * 4 + i;
+      const bool ok = row < N;
+      const float yv = ok ? y[row] : 0.f;
+      float rv[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float z = acc[i][j];
+        // bernoulli.py:126-140: -softplus(z) (1 - y) - softplus(-z) y
+        const float lp = -softplusf(z) * (1.f - yv) - softplusf(-z) * yv;
+        lp_tile[j] += ok ? lp : 0.f;
+        rv[j] = ok ? (yv - sigmoidf_(z)) : 0.f;
+      }
+      *reinterpret_cast<float4*>(&Rs[(ty * 4 + i) * kCT + tx * 4]) =
+          make_float4(rv[0], rv[1], rv[2], rv[3]);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) lp_acc[j] += (double)lp_tile[j];
+    __syncthreads();
+    // Phase 2: G[c][d] += sum_r Rs[r][c] Xt[d][r].
+    for (int r = 0; r < kNT; ++r) {
+      const float4 rv4 = *reinterpret_cast<const float4*>(&Rs[r * kCT + cg * 4]);
+      const float ra[4] = {rv4.x, rv4.y, rv4.z, rv4.w};
+#pragma unroll
+      for (int k = 0; k < KD; ++k) {
+        const float xv = Xt[(dg + 16 * k) * kXPad + r];
+#pragma unroll
+        for (int j = 0; j < 4; ++j) g[j][k] = fmaf(ra[j], xv, g[j][k]);
+      }
+    }
+  }
+
+  // Partial log-likelihood: reduce the 16 row groups (ty) of each chain.
+#pragma unroll
+  for (int j = 0; j < 4; ++j) red[ty][tx][j] = lp_acc[j];
+  __syncthreads();
+  if (tid < kCT) {
+    const int c = tid;
+    double s = 0.0;
+    for (int t = 0; t < kThreads / 16; ++t) s += red[t][c >> 2][c & 3];
+    if (c0 + c < n) lpart[(size_t)split * n + c0 + c] = s;
+  }
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const int c = c0 + cg * 4 + j;
+    if (c >= n) continue;
+    float* dst = gpart + ((size_t)split * n + c) * D;
+#pragma unroll
+    for (int k = 0; k < KD; ++k) {
+      const int d = dg + 16 * k;
+      if (d < D) dst[d] = g[j][k];
+    }
+  }
+}
+
+// One warp per state: sum the split partials in fixed order, add the prior.
+__global__ void logreg_reduce_kernel(const double* __restrict__ lpart,
+                                     const float* __restrict__ gpart, const float* __restrict__ Q,
+                                     int ldq, const int* __restrict__ n_dev, int grid, int N,
+                                     int D, float inv_var, double log_norm,
+                                     double* __restrict__ logp, float* __restrict__ grad, int ldg) {
+  const int n = *n_dev;
+  const int row_tiles = (N + kNT - 1) / kNT;
+  const int S = num_splits(n, grid, row_tiles);
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const float* q = Q + (size_t)warp * ldq;
+  double prior = 0.0;
+  for (int d = lane; d < D; d += 32) {
+    const float qd = q[d];
+    float acc = 0.f;
+    for (int s = 0; s < S; ++s) acc += gpart[((size_t)s * n + warp) * D + d];
+    grad[(size_t)warp * ldg + d] = acc - qd * inv_var;
+    prior += (double)qd * (double)qd;
+  }
+  prior = warp_sum(prior);
+  if (lane == 0) {
+    double lp = 0.0;
+    for (int s = 0; s < S; ++s) lp += lpart[(size_t)s * n + warp];
+    logp[warp] = lp - 0.5 * (double)inv_var * prior + (double)D * log_norm;
+  }
+}
+
+class LogregSimt final : public Target {
+ public:
+  LogregSimt(gbm_context* ctx, const float* X, int64_t n, int64_t d, const float* y,
+             float prior_scale)
+      : N_(n), D_(d) {
+    dim = d;
+    ldx_ = (int)((d + 3) / 4 * 4);
+    x_.reserve(sizeof(float) * (size_t)N_ * ldx_);
+    y_.reserve(sizeof(float) * (size_t)N_);
+    GBM_CUDA(cudaMemset2DAsync(x_.ptr, sizeof(float) * ldx_, 0, sizeof(float) * ldx_, N_,
+                               ctx->stream));
+    GBM_CUDA(cudaMemcpy2DAsync(x_.ptr, sizeof(float) * ldx_, X, sizeof(float) * d,
+                               sizeof(float) * d, N_, cudaMemcpyDeviceToDevice, ctx->stream));
+    GBM_CUDA(cudaMemcpyAsync(y_.ptr, y, sizeof(float) * N_, cudaMemcpyDeviceToDevice,
+                             ctx->stream));
+    inv_var_ = 1.f / (prior_scale * prior_scale);
+    log_norm_ = -log((double)prior_scale) - 0.5 * log(2.0 * M_PI);
+    grid_ = 2 * ctx->num_sms;
+    kd_ = d <= 32 ? 2 : d <= 64 ? 4 : d <= 128 ? 8 : 16;
+    smem_ = sizeof(float) * (size_t)(kd_ * 16) * (kCT + kXPad) + sizeof(float) * kNT * kCT;
+    set_smem(kd_);
+  }
+
+  size_t workspace_bytes(int64_t cap) const override {
+    const size_t rows = (size_t)grid_ * kCT + (size_t)cap;  // S * n <= grid * kCT + n
+    return rows * sizeof(double) + rows * (size_t)D_ * sizeof(float) + 256;
+  }
+
+  void eval(const float* q, int ldq, const int* n_dev, int cap, double* logp, float* grad,
+            int ldg, void* ws, cudaStream_t s) override {
+    const size_t rows = (size_t)grid_ * kCT + (size_t)cap;
+    double* lpart = static_cast<double*>(ws);
+    float* gpart = reinterpret_cast<float*>(lpart + rows);
+    const int N = (int)N_, D = (int)D_;
+    switch (kd_) {
+      case 2: logreg_partial_kernel<2><<<grid_, kThreads, smem_, s>>>(
+          x_.as<float>(), ldx_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart); break;
+      case 4: logreg_partial_kernel<4><<<grid_, kThreads, smem_, s>>>(
+          x_.as<float>(), ldx_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart); break;
+      case 8: logreg_partial_kernel<8><<<grid_, kThreads, smem_, s>>>(
+          x_.as<float>(), ldx_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart); break;
+      default: logreg_partial_kernel<16><<<grid_, kThreads, smem_, s>>>(
+          x_.as<float>(), ldx_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart); break;
+    }
+    GBM_CUDA(cudaGetLastError());
+    const int warps_per_block = 8;
+    logreg_reduce_kernel<<<(cap + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0,
+                           s>>>(lpart, gpart, q, ldq, n_dev, grid_, N, D, inv_var_, log_norm_,
+                                logp, grad, ldg);
+    GBM_CUDA(cudaGetLastError());
+  }
+
+  int launches_per_eval() const override { return 2; }
+  double flops(int64_t n) const override { return 4.0 * (double)N_ * D_ * n; }
+  double bytes(int64_t n) const override {
+    return 4.0 * (double)N_ * D_ + 4.0 * N_ + 8.0 * (double)n * D_ + 8.0 * n;
+  }
+
+ private:
+  void set_smem(int kd) {
+    const void* fn = kd == 2 ? (const void*)logreg_partial_kernel<2>
+                   : kd == 4 ? (const void*)logreg_partial_kernel<4>
+                   : kd == 8 ? (const void*)logreg_partial_kernel<8>
+                             : (const void*)logreg_partial_kernel<16>;
+    GBM_CUDA(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_));
+  }
+
+  int64_t N_, D_;
+  int ldx_ = 0, grid_ = 0, kd_ = 0;
+  size_t smem_ = 0;
+  float inv_var_ = 1.f;
+  double log_norm_ = 0.0;
+  DeviceBuffer x_, y_;
+};
+
+}  // namespace
+
+std::unique_ptr<Target> make_logreg_simt(gbm_context* ctx, const float* X, int64_t n, int64_t d,
+                                         const float* y, float prior_scale) {
+  if (d > 256) return nullptr;
+  return std::unique_ptr<Target>(new LogregSimt(ctx, X, n, d, y, prior_scale));
+}
+
+}  // namespace gbm

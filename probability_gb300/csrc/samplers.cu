@@ -1,0 +1,698 @@
+// HMC, NUTS and dual-averaging kernels plus their host-side orchestration.
+//
+// Chains live in chain-major [C][D] float32 arrays; log-densities, energies,
+// NUTS log-weights and energy-difference sums are float64.  Each per-chain
+// kernel runs one warp per chain with lanes striding over D.
+//
+// NUTS follows the reference's unrolled iterative formulation
+// (tensorflow_probability/python/mcmc/nuts.py:321-1102): multinomial
+// sampling, generalised U-turn criterion with the precomputed write/read slot
+// tables.  Unlike the reference's lock-step batch, only chains whose subtree
+// is still growing are evaluated: after every leaf the active chains are
+// compacted into a dense batch, so the gradient kernels never spend work on
+// finished chains.  Per-chain results are unchanged by this (a finished
+// chain's outputs are frozen in the reference, nuts.py:829-933), and draws
+// are addressed by (chain, depth, leaf) so compaction does not shift them.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "rng.cuh"
+#include "samplers.h"
+
+namespace gbm {
+
+constexpr int kWarpsPerBlock = 8;
+
+static inline int warp_blocks(int64_t n) {
+  return (int)((n + kWarpsPerBlock - 1) / kWarpsPerBlock);
+}
+
+__device__ __forceinline__ int warp_id() {
+  return (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+}
+
+__device__ __forceinline__ float eps_of(const float* eps, int per_chain, int c) {
+  return per_chain ? eps[c] : eps[0];
+}
+
+// --------------------------------------------------------------------------
+// Active-chain compaction: idx[0..count) = chains with (flags & bit), sorted.
+// --------------------------------------------------------------------------
+__global__ void build_active_kernel(const uint8_t* __restrict__ flags, uint8_t bit, int C,
+                                    int* __restrict__ idx, int* __restrict__ count) {
+  __shared__ int warp_tot[32];
+  __shared__ int base_s;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  if (tid == 0) base_s = 0;
+  __syncthreads();
+  for (int start = 0; start < C; start += blockDim.x) {
+    const int c = start + tid;
+    const bool on = c < C && (flags[c] & bit);
+    const unsigned m = __ballot_sync(0xffffffffu, on);
+    if (lane == 0) warp_tot[w] = __popc(m);
+    __syncthreads();
+    if (w == 0) {
+      int v = lane < (int)(blockDim.x >> 5) ? warp_tot[lane] : 0;
+      int incl = v;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int t = __shfl_up_sync(0xffffffffu, incl, o);
+        if (lane >= o) incl += t;
+      }
+      if (lane < (int)(blockDim.x >> 5)) warp_tot[lane] = incl - v;  // exclusive
+    }
+    __syncthreads();
+    const int base = base_s;
+    if (on) idx[base + warp_tot[w] + __popc(m & ((1u << lane) - 1u))] = c;
+    __syncthreads();
+    if (tid == blockDim.x - 1) {
+      const unsigned mm = m;  // last warp's ballot
+      base_s = base + warp_tot[w] + __popc(mm);
+    }
+    __syncthreads();
+  }
+  if (tid == 0) *count = base_s;
+}
+
+static void build_active(const NutsDev& d, uint8_t bit, cudaStream_t s) {
+  build_active_kernel<<<1, 1024, 0, s>>>(d.flags, bit, d.C, d.act_idx, d.act_count);
+  GBM_CUDA(cudaGetLastError());
+}
+
+// --------------------------------------------------------------------------
+// NUTS kernels
+// --------------------------------------------------------------------------
+__global__ void nuts_init_kernel(NutsDev w, const float* __restrict__ q,
+                                 const double* __restrict__ l, const float* __restrict__ g,
+                                 const float* __restrict__ eps_in, int eps_per_chain, uint2 key) {
+  const int c = warp_id(), lane = threadIdx.x & 31;
+  if (c >= w.C) return;
+  const int D = w.D;
+  const size_t o = (size_t)c * D;
+  const uint32_t site = draw_site(kDrawMomentum, 0, 0);
+  double kin = 0.0;
+  for (int d = lane; d < D; d += 32) {
+    const float p = draw_normal(key, site, (uint32_t)(o + d));
+    const float qd = q[o + d], gd = g[o + d];
+    w.end_q[0][o + d] = qd; w.end_q[1][o + d] = qd;
+    w.end_p[0][o + d] = p;  w.end_p[1][o + d] = p;
+    w.end_g[0][o + d] = gd; w.end_g[1][o + d] = gd;
+    w.cand_q[o + d] = qd;   w.cand_g[o + d] = gd;
+    w.mom_sum[o + d] = p;
+    kin += (double)p * (double)p;
+  }
+  kin = warp_sum(kin);
+  if (lane == 0) {
+    const double lc = l[c];
+    const double e0 = lc - 0.5 * kin;   // nuts.py:1085-1102 (negative energy)
+    w.end_l[0][c] = lc; w.end_l[1][c] = lc;
+    w.cand_l[c] = lc; w.cand_e[c] = e0; w.cand_w[c] = 0.0;
+    w.e0[c] = e0; w.eds[c] = 0.0; w.lf[c] = 0; w.tree_depth[c] = 0;
+    w.flags[c] = kCont | kNotDiv;
+    w.eps[c] = eps_of(eps_in, eps_per_chain, c);
+  }
+}
+
+__global__ void nuts_depth_begin_kernel(NutsDev w, uint2 key, int depth) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *w.any_cont = 0;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= w.C) return;
+  uint8_t f = w.flags[c];
+  if (!(f & kCont)) {
+    w.flags[c] = f & (uint8_t)~(kSubCont | kForward);
+    return;
+  }
+  const int fwd = draw_direction(key, (uint32_t)depth, (uint32_t)c);   // nuts.py:551-558
+  f = (f & (uint8_t)~(kForward | kSubNotDiv)) | kSubCont | (fwd ? kForward : 0) |
+      ((f & kNotDiv) ? kSubNotDiv : 0);
+  w.flags[c] = f;
+  w.sub_w[c] = -INFINITY;               // nuts.py:727-731
+  w.sub_eds[c] = 0.0;
+  w.sub_lf[c] = 0;
+  w.tree_depth[c] += 1;
+}
+
+__global__ void nuts_zero_cumsum_kernel(NutsDev w) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t n = (size_t)w.C * w.D;
+  if (i < n && (w.flags[i / w.D] & kSubCont)) w.cumsum[i] = 0.f;
+}
+
+// Half kick + drift for the active chains; writes the dense batch qw.
+// leapfrog_integrator.py:280-286 (half kick) and :330-334 (drift).
+__global__ void nuts_leaf_pre_kernel(NutsDev w) {
+  const int j = warp_id(), lane = threadIdx.x & 31;
+  if (j >= *w.act_count) return;
+  const int c = w.act_idx[j];
+  const int side = (w.flags[c] & kForward) ? 1 : 0;
+  const float e = (side ? 1.f : -1.f) * w.eps[c];
+  const float he = 0.5f * e;
+  const size_t o = (size_t)c * w.D, oj = (size_t)j * w.D;
+  float* P = w.end_p[side];
+  float* Q = w.end_q[side];
+  const float* G = w.end_g[side];
+  for (int d = lane; d < w.D; d += 32) {
+    const float ph = P[o + d] + he * G[o + d];
+    const float qn = Q[o + d] + e * ph;
+    P[o + d] = ph;
+    Q[o + d] = qn;
+    w.qw[oj + d] = qn;
+  }
+}
+
+// Between the unrolled leapfrog steps of one leaf: full kick then drift.
+__global__ void nuts_leaf_mid_kernel(NutsDev w) {
+  const int j = warp_id(), lane = threadIdx.x & 31;
+  if (j >= *w.act_count) return;
+  const int c = w.act_idx[j];
+  const int side = (w.flags[c] & kForward) ? 1 : 0;
+  const float e = (side ? 1.f : -1.f) * w.eps[c];
+  const size_t o = (size_t)c * w.D, oj = (size_t)j * w.D;
+  for (int d = lane; d < w.D; d += 32) {
+    const float ph = w.end_p[side][o + d] + e * w.gw[oj + d];
+    const float qn = w.end_q[side][o + d] + e * ph;
+    w.end_p[side][o + d] = ph;
+    w.end_q[side][o + d] = qn;
+    w.qw[oj + d] = qn;
+  }
+}
+
+// Final kick, slot bookkeeping, U-turn checks, energy, multinomial leaf
+// sampling: _loop_build_sub_tree (nuts.py:793-946) and
+// has_not_u_turn_at_all_index (nuts.py:949-984).
+__global__ void nuts_leaf_post_kernel(NutsDev w, uint2 key, int depth, int leaf, int wslot,
+                                      int r0, int r1, double max_energy_diff) {
+  const int j = warp_id(), lane = threadIdx.x & 31;
+  if (j >= *w.act_count) return;
+  const int c = w.act_idx[j];
+  const int D = w.D;
+  const uint8_t f = w.flags[c];
+  const int side = (f & kForward) ? 1 : 0;
+  const float e = (side ? 1.f : -1.f) * w.eps[c];
+  const float he = 0.5f * e;
+  const size_t o = (size_t)c * D, oj = (size_t)j * D;
+  float* P = w.end_p[side];
+  float* Gs = w.end_g[side];
+  double kin = 0.0;
+  for (int d = lane; d < D; d += 32) {
+    const float g2 = w.gw[oj + d];
+    const float p2 = (P[o + d] + e * g2) - he * g2;   // leapfrog_integrator.py:345-349,:304-309
+    P[o + d] = p2;
+    Gs[o + d] = g2;
+    const float csp = w.cumsum[o + d];
+    const float cs = csp + p2;                          // nuts.py:827-828
+    w.cumsum[o + d] = cs;
+    if (wslot >= 0) {                                   // nuts.py:857-869
+      const size_t so = ((size_t)c * w.slots + wslot) * D + d;
+      w.slot_p[so] = p2;
+      w.slot_cs[so] = csp;
+    }
+    kin += (double)p2 * (double)p2;
+  }
+  kin = warp_sum(kin);
+  __syncwarp();
+  // Within-subtree U-turn over the read range (reads never hit wslot: a leaf
+  // that ends subtrees writes only the dummy slot, which is skipped).
+  bool no_uturn = true;
+  for (int i = r0; i < r1; ++i) {
+    double dl = 0.0, dr = 0.0;
+    const size_t so = ((size_t)c * w.slots + i) * D;
+    for (int d = lane; d < D; d += 32) {
+      const float diff = w.cumsum[o + d] - w.slot_cs[so + d];
+      dl += (double)diff * (double)w.slot_p[so + d];
+      dr += (double)diff * (double)P[o + d];
+    }
+    dl = warp_sum(dl);
+    dr = warp_sum(dr);
+    no_uturn = no_uturn && (dl >= 0.0) && (dr >= 0.0);
+  }
+  const double l2 = w.lw[j];
+  double energy = l2 - 0.5 * kin;                         // nuts.py:871-876
+  if (isnan(energy)) energy = -INFINITY;
+  const double de = energy - w.e0[c];
+  const bool not_div = -de < max_energy_diff;             // nuts.py:880
+  const double wsum = log_add_exp(w.sub_w[c], de);        // nuts.py:881-883
+  const double thresh = de - wsum;
+  const float U = draw_uniform(key, draw_site(kDrawLeafUniform, depth, leaf), (uint32_t)c);
+  const bool acc = log1p(-(double)U) <= thresh;           // nuts.py:897-901
+  if (acc) {
+    for (int d = lane; d < D; d += 32) {
+      w.sub_q[o + d] = w.end_q[side][o + d];
+      w.sub_g[o + d] = Gs[o + d];
+    }
+  }
+  if (lane == 0) {
+    w.end_l[side][c] = l2;
+    if (acc) { w.sub_l[c] = l2; w.sub_e[c] = energy; }
+    w.sub_w[c] = wsum;
+    const bool cont = not_div;                            // previous was active
+    if (cont) w.sub_eds[c] += exp(fmin(de, 0.0));         // nuts.py:929-933
+    w.sub_lf[c] += 1;                                     // nuts.py:829-830
+    uint8_t nf = f;
+    if (!not_div) nf &= (uint8_t)~kSubNotDiv;
+    if (!(cont && no_uturn)) nf &= (uint8_t)~kSubCont;
+    w.flags[c] = nf;
+  }
+}
+
+// Tree-level biased progressive sampling and trajectory U-turn check
+// (nuts.py:597-711).
+__global__ void nuts_depth_end_kernel(NutsDev w, uint2 key, int depth) {
+  const int c = warp_id(), lane = threadIdx.x & 31;
+  if (c >= w.C) return;
+  const uint8_t f = w.flags[c];
+  if (!(f & kCont)) return;
+  const int D = w.D;
+  const size_t o = (size_t)c * D;
+  const bool sub_cont = f & kSubCont;
+  const double tree_w = sub_cont ? w.sub_w[c] : -INFINITY;
+  const double cw = w.cand_w[c];
+  const double wsum = log_add_exp(tree_w, cw);
+  double thresh = tree_w - cw;
+  if (isnan(thresh)) thresh = 0.0;
+  const float U = draw_uniform(key, draw_site(kDrawTreeUniform, depth, 0), (uint32_t)c);
+  const bool choose = (log1p(-(double)U) <= thresh) && sub_cont;
+  double dl = 0.0, dr = 0.0;
+  for (int d = lane; d < D; d += 32) {
+    if (choose) {
+      w.cand_q[o + d] = w.sub_q[o + d];
+      w.cand_g[o + d] = w.sub_g[o + d];
+    }
+    const float ms = w.mom_sum[o + d] + w.cumsum[o + d];
+    w.mom_sum[o + d] = ms;
+    dl += (double)ms * (double)w.end_p[0][o + d];
+    dr += (double)ms * (double)w.end_p[1][o + d];
+  }
+  dl = warp_sum(dl);
+  dr = warp_sum(dr);
+  if (lane == 0) {
+    if (choose) { w.cand_l[c] = w.sub_l[c]; w.cand_e[c] = w.sub_e[c]; }
+    w.cand_w[c] = wsum;
+    w.eds[c] += w.sub_eds[c];
+    w.lf[c] += w.sub_lf[c];
+    const bool no_uturn = dl >= 0.0 && dr >= 0.0;
+    uint8_t nf = f;
+    if (choose) nf |= kAccepted;
+    if (!(sub_cont && no_uturn)) nf &= (uint8_t)~kCont;
+    nf = (f & kSubNotDiv) ? (nf | kNotDiv) : (nf & (uint8_t)~kNotDiv);
+    w.flags[c] = nf;
+    if (nf & kCont) atomicOr(w.any_cont, 1);
+  }
+}
+
+__global__ void nuts_finalize_kernel(NutsDev w, NutsOutputs out, int unrolled) {
+  const int c = warp_id(), lane = threadIdx.x & 31;
+  if (c >= w.C) return;
+  const size_t o = (size_t)c * w.D;
+  for (int d = lane; d < w.D; d += 32) {
+    out.state[o + d] = w.cand_q[o + d];
+    out.grads[o + d] = w.cand_g[o + d];
+  }
+  if (lane == 0) {
+    const uint8_t f = w.flags[c];
+    out.target_log_prob[c] = w.cand_l[c];
+    out.log_accept_ratio[c] = log(w.eds[c] / (double)w.lf[c]);   // nuts.py:429-432
+    out.leapfrogs_taken[c] = w.lf[c] * unrolled;
+    out.is_accepted[c] = (f & kAccepted) ? 1 : 0;
+    out.reach_max_depth[c] = (f & kCont) ? 1 : 0;
+    out.has_divergence[c] = (f & kNotDiv) ? 0 : 1;
+    out.energy[c] = w.cand_e[c];
+    if (out.tree_depth) out.tree_depth[c] = w.tree_depth[c];
+  }
+}
+
+// --------------------------------------------------------------------------
+// HMC kernels: UncalibratedHamiltonianMonteCarlo + MetropolisHastings.
+// --------------------------------------------------------------------------
+struct HmcDev {
+  int C, D;
+  float *p0, *ph, *qw, *gw;
+  double* lw;
+  int* count;
+};
+
+__global__ void hmc_init_kernel(HmcDev w, const float* __restrict__ q, const float* __restrict__ g,
+                                const float* __restrict__ eps, int per_chain, uint2 key) {
+  const int c = warp_id(), lane = threadIdx.x & 31;
+  if (c >= w.C) return;
+  if (c == 0 && lane == 0) *w.count = w.C;
+  const float e = eps_of(eps, per_chain, c), he = 0.5f * e;
+  const size_t o = (size_t)c * w.D;
+  const uint32_t site = draw_site(kDrawMomentum, 0, 0);
+  for (int d = lane; d < w.D; d += 32) {
+    const float p = draw_normal(key, site, (uint32_t)(o + d));   // hmc.py:684-695
+    w.p0[o + d] = p;
+    const float ph = p + he * g[o + d];
+    w.ph[o + d] = ph;
+    w.qw[o + d] = q[o + d] + e * ph;
+  }
+}
+
+__global__ void hmc_kick_drift_kernel(HmcDev w, const float* __restrict__ eps, int per_chain) {
+  const int c = warp_id(), lane = threadIdx.x & 31;
+  if (c >= w.C) return;
+  const float e = eps_of(eps, per_chain, c);
+  const size_t o = (size_t)c * w.D;
+  for (int d = lane; d < w.D; d += 32) {
+    const float ph = w.ph[o + d] + e * w.gw[o + d];
+    w.ph[o + d] = ph;
+    w.qw[o + d] = w.qw[o + d] + e * ph;
+  }
+}
+
+__global__ void hmc_finish_kernel(HmcDev w, const float* __restrict__ q0,
+                                  const double* __restrict__ l0, const float* __restrict__ g0,
+                                  const float* __restrict__ eps, int per_chain, uint2 key,
+                                  HmcOutputs out) {
+  const int c = warp_id(), lane = threadIdx.x & 31;
+  if (c >= w.C) return;
+  const float e = eps_of(eps, per_chain, c), he = 0.5f * e;
+  const size_t o = (size_t)c * w.D;
+  double k0 = 0.0, k1 = 0.0;
+  for (int d = lane; d < w.D; d += 32) {
+    const float g = w.gw[o + d];
+    const float p1 = (w.ph[o + d] + e * g) - he * g;
+    const float p0 = w.p0[o + d];
+    k0 += (double)p0 * (double)p0;
+    k1 += (double)p1 * (double)p1;
+    if (out.final_momentum) out.final_momentum[o + d] = p1;
+    if (out.initial_momentum) out.initial_momentum[o + d] = p0;
+    if (out.proposed_state) out.proposed_state[o + d] = w.qw[o + d];
+    if (out.proposed_grads) out.proposed_grads[o + d] = g;
+  }
+  k0 = warp_sum(k0);
+  k1 = warp_sum(k1);
+  const double l1 = w.lw[c];
+  double corr = k0 - k1;                                  // hmc.py:861-875
+  corr = isfinite(corr) ? 0.5 * corr : -INFINITY;
+  double lar = l1 - l0[c] + corr;                         // metropolis_hastings.py:204-215
+  if (!isfinite(lar)) lar = -INFINITY;
+  const float U = draw_uniform(key, draw_site(kDrawMhUniform, 0, 0), (uint32_t)c);
+  const bool acc = log((double)U) < lar;                  // metropolis_hastings.py:221-227
+  for (int d = lane; d < w.D; d += 32) {
+    out.next_state[o + d] = acc ? w.qw[o + d] : q0[o + d];
+    out.next_grads[o + d] = acc ? w.gw[o + d] : g0[o + d];
+  }
+  if (lane == 0) {
+    out.next_tlp[c] = acc ? l1 : l0[c];
+    if (out.proposed_tlp) out.proposed_tlp[c] = l1;
+    if (out.log_acceptance_correction) out.log_acceptance_correction[c] = corr;
+    out.log_accept_ratio[c] = lar;
+    out.is_accepted[c] = acc ? 1 : 0;
+  }
+}
+
+// --------------------------------------------------------------------------
+// Dual averaging (dual_averaging_step_size_adaptation.py:353-475)
+// --------------------------------------------------------------------------
+// state: [groups][4] doubles = error_sum, log_averaging_step, log_shrinkage_target, step.
+__global__ void dual_averaging_kernel(const double* __restrict__ lar, int C, int per_chain,
+                                      DaParams prm, const double* __restrict__ target_accept,
+                                      double* __restrict__ state, float* __restrict__ eps) {
+  __shared__ double red[32];
+  __shared__ double bcast;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  const int nw = (blockDim.x + 31) >> 5;
+  auto lap = [&](int c) {  // simple_step_size_adaptation.py:42-48
+    double v = lar[c];
+    if (!isfinite(v)) v = -INFINITY;
+    return fmin(v, 0.0);
+  };
+  auto update = [&](int g, double reduced) {
+    double* st = state + 4 * g;
+    const double tgt = target_accept ? target_accept[g] : prm.target_accept_prob;
+    const double err = st[0] + tgt - exp(reduced);
+    const double step = st[3] + 1.0;
+    const double soft_t = prm.step_count_smoothing + step;
+    const double new_log_step = st[2] - (err * sqrt(step)) / (soft_t * prm.exploration_shrinkage);
+    const double eta = pow(step, -prm.decay_rate);
+    double new_log_avg = eta * new_log_step + (1.0 - eta) * st[1];
+    const int istep = (int)step;
+    const float cur = eps[g];
+    float ns;
+    if (istep < prm.num_adaptation_steps) ns = (float)exp(new_log_step);
+    else if (istep > prm.num_adaptation_steps) ns = cur;
+    else ns = (float)exp(new_log_avg);
+    if (istep > prm.num_adaptation_steps) new_log_avg = st[1];
+    st[0] = err;
+    st[1] = new_log_avg;
+    st[3] = step;
+    eps[g] = ns;
+  };
+  if (per_chain) {
+    for (int c = tid; c < C; c += blockDim.x) update(c, lap(c));
+    return;
+  }
+  // reduce_logmeanexp over all chains (math/generic.py:221-275).
+  double m = -INFINITY;
+  for (int c = tid; c < C; c += blockDim.x) m = fmax(m, lap(c));
+  for (int o = 16; o > 0; o >>= 1) m = fmax(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if (lane == 0) red[wid] = m;
+  __syncthreads();
+  if (tid == 0) {
+    double mm = -INFINITY;
+    for (int i = 0; i < nw; ++i) mm = fmax(mm, red[i]);
+    bcast = isfinite(mm) ? mm : 0.0;
+  }
+  __syncthreads();
+  const double mx = bcast;
+  double s = 0.0;
+  for (int c = tid; c < C; c += blockDim.x) s += exp(lap(c) - mx);
+  s = warp_sum(s);
+  __syncthreads();
+  if (lane == 0) red[wid] = s;
+  __syncthreads();
+  if (tid == 0) {
+    double tot = 0.0;
+    for (int i = 0; i < nw; ++i) tot += red[i];
+    update(0, log(tot) + mx - log((double)C));
+  }
+}
+
+// --------------------------------------------------------------------------
+// Host orchestration
+// --------------------------------------------------------------------------
+
+// nuts.py:1013-1071, restated: the slot each leaf writes (-1: nothing to
+// keep) and the slot range [lo, hi) it checks for a U-turn.
+void nuts_instructions(int depth, std::vector<int>* write, std::vector<int>* lo,
+                       std::vector<int>* hi, int* slots) {
+  const int n = 1 << depth;
+  std::vector<int> last_end(n, -1);
+  std::vector<std::vector<int>> ends_at(n);
+  for (int h = 1; h <= depth; ++h) {
+    const int size = 1 << h;
+    for (int a = 0; a < n; a += size) {
+      last_end[a] = std::max(last_end[a], a + size - 1);
+      ends_at[a + size - 1].push_back(a);
+    }
+  }
+  write->assign(n, -1);
+  lo->assign(n, 0);
+  hi->assign(n, 0);
+  int max_slot = 0;
+  for (int j = 0; j < n; ++j) {
+    std::vector<int> alive;
+    for (int i = 0; i <= j; ++i)
+      if (last_end[i] >= j) alive.push_back(i);
+    if (last_end[j] >= 0) {
+      (*write)[j] = (int)alive.size() - 1;
+      max_slot = std::max(max_slot, (*write)[j]);
+    }
+    if (!ends_at[j].empty()) {
+      const int first = *std::min_element(ends_at[j].begin(), ends_at[j].end());
+      const int r0 = (int)(std::find(alive.begin(), alive.end(), first) - alive.begin());
+      (*lo)[j] = r0;
+      (*hi)[j] = r0 + (int)ends_at[j].size();
+    }
+  }
+  *slots = max_slot + 1;
+}
+
+void nuts_setup(gbm_nuts* k) {
+  int slots = 0;
+  nuts_instructions(k->max_tree_depth, &k->write_instr, &k->read_lo, &k->read_hi, &slots);
+  const int64_t C = k->max_chains, D = k->target->impl->dim;
+  NutsDev& w = k->dev;
+  w.C = (int)C;
+  w.D = (int)D;
+  w.slots = slots;
+  // Carve one allocation: float vectors, slot memory, doubles, ints, bytes.
+  const size_t vec = (size_t)C * D;
+  const size_t n_float_vecs = 6 + 6 + 2;   // ends(6), cand/sub/mom/cumsum(6), qw/gw(2)
+  size_t bytes = 0;
+  auto take = [&](size_t b) { size_t at = bytes; bytes += (b + 255) / 256 * 256; return at; };
+  size_t off_f = take(sizeof(float) * vec * n_float_vecs);
+  size_t off_slots = take(sizeof(float) * vec * slots * 2);
+  size_t off_d = take(sizeof(double) * C * 12);
+  size_t off_i = take(sizeof(int) * C * 4 + 64);
+  size_t off_b = take(C);
+  size_t off_e = take(sizeof(float) * C);
+  k->mem.reserve(bytes);
+  char* base = k->mem.as<char>();
+  float* fv = reinterpret_cast<float*>(base + off_f);
+  w.end_q[0] = fv + 0 * vec; w.end_q[1] = fv + 1 * vec;
+  w.end_p[0] = fv + 2 * vec; w.end_p[1] = fv + 3 * vec;
+  w.end_g[0] = fv + 4 * vec; w.end_g[1] = fv + 5 * vec;
+  w.cand_q = fv + 6 * vec; w.cand_g = fv + 7 * vec;
+  w.sub_q = fv + 8 * vec; w.sub_g = fv + 9 * vec;
+  w.mom_sum = fv + 10 * vec; w.cumsum = fv + 11 * vec;
+  w.qw = fv + 12 * vec; w.gw = fv + 13 * vec;
+  float* sv = reinterpret_cast<float*>(base + off_slots);
+  w.slot_p = sv;
+  w.slot_cs = sv + vec * slots;
+  double* dv = reinterpret_cast<double*>(base + off_d);
+  w.end_l[0] = dv + 0 * C; w.end_l[1] = dv + 1 * C;
+  w.cand_l = dv + 2 * C; w.cand_e = dv + 3 * C; w.cand_w = dv + 4 * C;
+  w.sub_l = dv + 5 * C; w.sub_e = dv + 6 * C; w.sub_w = dv + 7 * C;
+  w.e0 = dv + 8 * C; w.eds = dv + 9 * C; w.sub_eds = dv + 10 * C; w.lw = dv + 11 * C;
+  int* iv = reinterpret_cast<int*>(base + off_i);
+  w.lf = iv; w.sub_lf = iv + C; w.tree_depth = iv + 2 * C; w.act_idx = iv + 3 * C;
+  w.act_count = iv + 4 * C; w.any_cont = iv + 4 * C + 1;
+  w.flags = reinterpret_cast<uint8_t*>(base + off_b);
+  w.eps = reinterpret_cast<float*>(base + off_e);
+  GBM_CUDA(cudaMemset(base, 0, bytes));
+  k->target_ws.reserve(k->target->impl->workspace_bytes(C));
+  for (auto& ev : k->poll_events) GBM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+}
+
+static void nuts_eval(gbm_nuts* k, cudaStream_t s) {
+  const NutsDev& w = k->dev;
+  if (k->profiling) {
+    if (k->prof_used + 2 > k->prof_events.size()) {
+      cudaEvent_t a, b;
+      GBM_CUDA(cudaEventCreate(&a));
+      GBM_CUDA(cudaEventCreate(&b));
+      k->prof_events.push_back(a);
+      k->prof_events.push_back(b);
+    }
+    GBM_CUDA(cudaEventRecord(k->prof_events[k->prof_used], s));
+  }
+  k->target->impl->eval(w.qw, w.D, w.act_count, w.C, w.lw, w.gw, w.D, k->target_ws.ptr, s);
+  k->prof_launches += k->target->impl->launches_per_eval();
+  if (k->profiling) {
+    GBM_CUDA(cudaEventRecord(k->prof_events[k->prof_used + 1], s));
+    k->prof_used += 2;
+    ++k->prof_evals;
+  }
+}
+
+// Sum the recorded (start, end) pairs; the stream must be synchronized.
+void nuts_profile_flush(gbm_nuts* k) {
+  for (size_t i = 0; i + 1 < k->prof_used; i += 2) {
+    float ms = 0.f;
+    GBM_CUDA(cudaEventElapsedTime(&ms, k->prof_events[i], k->prof_events[i + 1]));
+    k->prof_eval_ms += ms;
+  }
+  k->prof_used = 0;
+}
+
+void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l, const float* g,
+                   const float* eps, int eps_per_chain, uint2 key, const NutsOutputs& out) {
+  gbm_context* ctx = k->target->ctx;
+  cudaStream_t s = ctx->stream;
+  NutsDev w = k->dev;
+  w.C = (int)chains;
+  int* host_flags = ctx->host_flags;
+  const int wb = warp_blocks(chains), tb = 256;
+  nuts_init_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, q, l, g, eps, eps_per_chain, key);
+  GBM_CUDA(cudaGetLastError());
+  k->last_leaf_iterations = 0;
+  const size_t vec = (size_t)chains * w.D;
+  for (int depth = 0; depth < k->max_tree_depth; ++depth) {
+    if (depth > 0) {
+      GBM_CUDA(cudaMemcpyAsync(host_flags, w.any_cont, sizeof(int), cudaMemcpyDeviceToHost, s));
+      GBM_CUDA(cudaStreamSynchronize(s));
+      if (k->profiling) nuts_profile_flush(k);
+      if (host_flags[0] == 0) break;
+    }
+    nuts_depth_begin_kernel<<<(int)((chains + tb - 1) / tb), tb, 0, s>>>(w, key, depth);
+    nuts_zero_cumsum_kernel<<<(int)((vec + tb - 1) / tb), tb, 0, s>>>(w);
+    build_active(w, kSubCont, s);
+    const int leaves = 1 << depth;
+    const int batch = 8;
+    for (int leaf = 0; leaf < leaves; ++leaf) {
+      // Stop launching once every chain's subtree has terminated: poll the
+      // active count recorded at the previous batch boundary (the host runs
+      // at most one batch of leaves ahead of the device).
+      if (leaf % batch == 0 && leaf > 0) {
+        const int b = leaf / batch;
+        const int slot = b % 4;
+        GBM_CUDA(cudaMemcpyAsync(host_flags + 1 + slot, w.act_count, sizeof(int),
+                                 cudaMemcpyDeviceToHost, s));
+        GBM_CUDA(cudaEventRecord(k->poll_events[slot], s));
+        if (b >= 2) {
+          const int prev = (b - 1) % 4;
+          GBM_CUDA(cudaEventSynchronize(k->poll_events[prev]));
+          if (host_flags[1 + prev] == 0) break;
+        }
+      }
+      nuts_leaf_pre_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w);
+      nuts_eval(k, s);
+      for (int u = 1; u < k->unrolled_leapfrog_steps; ++u) {
+        nuts_leaf_mid_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w);
+        nuts_eval(k, s);
+      }
+      nuts_leaf_post_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(
+          w, key, depth, leaf, k->write_instr[leaf], k->read_lo[leaf], k->read_hi[leaf],
+          k->max_energy_diff);
+      GBM_CUDA(cudaGetLastError());
+      build_active(w, kSubCont, s);
+      ++k->last_leaf_iterations;
+      k->prof_launches += 3 + (k->unrolled_leapfrog_steps - 1);
+    }
+    nuts_depth_end_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, key, depth);
+    GBM_CUDA(cudaGetLastError());
+    k->prof_launches += 4;
+  }
+  nuts_finalize_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, out, k->unrolled_leapfrog_steps);
+  GBM_CUDA(cudaGetLastError());
+  k->prof_launches += 2;
+}
+
+void hmc_setup(gbm_hmc* k) {
+  const int64_t C = k->max_chains, D = k->target->impl->dim;
+  const size_t vec = (size_t)C * D;
+  k->mem.reserve(sizeof(float) * vec * 4 + sizeof(double) * C + 256 + sizeof(int) * 64);
+  k->target_ws.reserve(k->target->impl->workspace_bytes(C));
+}
+
+void hmc_one_step(gbm_hmc* k, int64_t chains, const float* q, const double* l, const float* g,
+                  const float* eps, int per_chain, int num_leapfrog_steps, uint2 key,
+                  const HmcOutputs& out) {
+  cudaStream_t s = k->target->ctx->stream;
+  const int64_t D = k->target->impl->dim;
+  const size_t vec = (size_t)k->max_chains * D;
+  float* fv = k->mem.as<float>();
+  HmcDev w;
+  w.C = (int)chains;
+  w.D = (int)D;
+  w.p0 = fv;
+  w.ph = fv + vec;
+  w.qw = fv + 2 * vec;
+  w.gw = fv + 3 * vec;
+  w.lw = reinterpret_cast<double*>(fv + 4 * vec);
+  w.count = reinterpret_cast<int*>(w.lw + k->max_chains);
+  const int wb = warp_blocks(chains);
+  hmc_init_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, q, g, eps, per_chain, key);
+  GBM_CUDA(cudaGetLastError());
+  for (int i = 0; i < num_leapfrog_steps; ++i) {
+    k->target->impl->eval(w.qw, w.D, w.count, w.C, w.lw, w.gw, w.D, k->target_ws.ptr, s);
+    if (i + 1 < num_leapfrog_steps)
+      hmc_kick_drift_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, eps, per_chain);
+  }
+  hmc_finish_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, q, l, g, eps, per_chain, key, out);
+  GBM_CUDA(cudaGetLastError());
+}
+
+void dual_averaging_update(cudaStream_t s, const double* lar, int64_t C, int per_chain,
+                           const DaParams& prm, const double* target_accept, double* state,
+                           float* eps) {
+  dual_averaging_kernel<<<1, 1024, 0, s>>>(lar, (int)C, per_chain, prm, target_accept, state, eps);
+  GBM_CUDA(cudaGetLastError());
+}
+
+}  // namespace gbm

@@ -1,0 +1,123 @@
+// Sampler workspaces and host orchestration (internal).
+#pragma once
+#include <stdint.h>
+
+#include <vector>
+
+#include "engine.h"
+
+namespace gbm {
+
+// Per-chain flags (one byte per chain).
+enum ChainFlag : uint8_t {
+  kCont = 1,        // trajectory still growing (continue_tree)
+  kNotDiv = 2,      // no divergence so far (not_divergence)
+  kAccepted = 4,    // a new candidate was chosen (is_accepted)
+  kSubCont = 8,     // current subtree still growing
+  kSubNotDiv = 16,  // subtree-level not_divergence
+  kForward = 32,    // direction of the current subtree
+};
+
+// Device pointers of the NUTS workspace (passed to kernels by value).
+struct NutsDev {
+  int C, D, slots;
+  float* end_q[2];
+  float* end_p[2];
+  float* end_g[2];
+  double* end_l[2];
+  float *cand_q, *cand_g, *sub_q, *sub_g, *mom_sum, *cumsum;
+  float *slot_p, *slot_cs;  // [C][slots][D]
+  float *qw, *gw;           // compacted batch [C][D]
+  double* lw;               // [C]
+  double *cand_l, *cand_e, *cand_w, *sub_l, *sub_e, *sub_w, *e0, *eds, *sub_eds;
+  int *lf, *sub_lf, *tree_depth;
+  uint8_t* flags;
+  float* eps;               // |step size| per chain
+  int* act_idx;             // [C]
+  int* act_count;           // [1]
+  int* any_cont;            // [1]
+};
+
+struct NutsOutputs {
+  float* state;
+  double* target_log_prob;
+  float* grads;
+  double* log_accept_ratio;
+  int32_t* leapfrogs_taken;
+  uint8_t* is_accepted;
+  uint8_t* reach_max_depth;
+  uint8_t* has_divergence;
+  double* energy;
+  int32_t* tree_depth;      // optional
+};
+
+struct HmcOutputs {
+  float* next_state;
+  double* next_tlp;
+  float* next_grads;
+  float* proposed_state;
+  double* proposed_tlp;
+  float* proposed_grads;
+  float* initial_momentum;
+  float* final_momentum;
+  double* log_acceptance_correction;
+  double* log_accept_ratio;
+  uint8_t* is_accepted;
+};
+
+struct DaParams {
+  double target_accept_prob, exploration_shrinkage, step_count_smoothing, decay_rate;
+  int num_adaptation_steps;
+};
+
+}  // namespace gbm
+
+struct gbm_nuts;
+struct gbm_hmc;
+
+namespace gbm {
+void nuts_setup(gbm_nuts* k);
+void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l, const float* g,
+                   const float* eps, int eps_per_chain, uint2 key, const NutsOutputs& out);
+void hmc_setup(gbm_hmc* k);
+void hmc_one_step(gbm_hmc* k, int64_t chains, const float* q, const double* l, const float* g,
+                  const float* eps, int per_chain, int num_leapfrog_steps, uint2 key,
+                  const HmcOutputs& out);
+void dual_averaging_update(cudaStream_t s, const double* lar, int64_t C, int per_chain,
+                           const DaParams& prm, const double* target_accept, double* state,
+                           float* eps);
+}  // namespace gbm
+
+struct gbm_nuts {
+  gbm_target* target = nullptr;
+  int64_t max_chains = 0;
+  int max_tree_depth = 10;
+  double max_energy_diff = 1000.0;
+  int unrolled_leapfrog_steps = 1;
+  std::vector<int> write_instr;             // per leaf (dummy = -1)
+  std::vector<int> read_lo, read_hi;        // per leaf
+  gbm::DeviceBuffer mem;
+  gbm::DeviceBuffer target_ws;
+  gbm::NutsDev dev{};
+  cudaEvent_t poll_events[4] = {nullptr, nullptr, nullptr, nullptr};
+  // Counters for the last transition (host-visible after one_step returns).
+  int64_t last_leaf_iterations = 0;
+  // Optional profiling: CUDA events bracket every batched target evaluation.
+  bool profiling = false;
+  std::vector<cudaEvent_t> prof_events;  // pairs (start, end)
+  size_t prof_used = 0;                  // events recorded since the last flush
+  double prof_eval_ms = 0.0;
+  int64_t prof_evals = 0;
+  int64_t prof_launches = 0;             // every kernel this handle launched
+};
+
+namespace gbm {
+void nuts_profile_flush(gbm_nuts* k);  // stream must be synchronized
+}  // namespace gbm
+
+struct gbm_hmc {
+  gbm_target* target = nullptr;
+  int64_t max_chains = 0;
+  gbm::DeviceBuffer mem;
+  gbm::DeviceBuffer target_ws;
+};

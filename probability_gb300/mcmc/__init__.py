@@ -1,0 +1,24 @@
+"""Drop-in subset of ``tfp.mcmc`` backed by the GB300 engine."""
+from probability_gb300.mcmc.diagnostic import effective_sample_size, potential_scale_reduction
+from probability_gb300.mcmc.dual_averaging_step_size_adaptation import (
+    DualAveragingStepSizeAdaptation, DualAveragingStepSizeAdaptationResults)
+from probability_gb300.mcmc.hmc import (HamiltonianMonteCarlo, UncalibratedHamiltonianMonteCarlo,
+                                        UncalibratedHamiltonianMonteCarloKernelResults)
+from probability_gb300.mcmc.kernel import TransitionKernel
+from probability_gb300.mcmc.metropolis_hastings import MetropolisHastingsKernelResults
+from probability_gb300.mcmc.nuts import NoUTurnSampler, NUTSKernelResults
+from probability_gb300.mcmc.sample import (CheckpointableStatesAndTrace, StatesAndTrace,
+                                           sample_chain)
+from probability_gb300.mcmc.simple_step_size_adaptation import (
+    hmc_like_log_accept_prob_getter_fn, hmc_like_step_size_getter_fn,
+    hmc_like_step_size_setter_fn)
+
+__all__ = [
+    'CheckpointableStatesAndTrace', 'DualAveragingStepSizeAdaptation',
+    'DualAveragingStepSizeAdaptationResults', 'HamiltonianMonteCarlo',
+    'MetropolisHastingsKernelResults', 'NUTSKernelResults', 'NoUTurnSampler', 'StatesAndTrace',
+    'TransitionKernel', 'UncalibratedHamiltonianMonteCarlo',
+    'UncalibratedHamiltonianMonteCarloKernelResults', 'effective_sample_size',
+    'hmc_like_log_accept_prob_getter_fn', 'hmc_like_step_size_getter_fn',
+    'hmc_like_step_size_setter_fn', 'potential_scale_reduction', 'sample_chain',
+]
