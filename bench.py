@@ -140,10 +140,11 @@ def cpu_baseline_run(w, X, y, init, max_seconds, steps_cap, state=None, step_siz
 
   def target(q):
     q = q.astype(np.float32)
-    z = q @ Xf.T
-    lp = -(np.logaddexp(0, z) * (1 - yf) + np.logaddexp(0, -z) * yf).sum(-1, dtype=np.float64)
+    z = q @ Xf.T                                   # [C, N]
+    sp = np.logaddexp(np.float32(0), z)            # softplus(z)
+    lp = (yf * z - sp).sum(-1, dtype=np.float64)   # bernoulli.py:126-140
     lp += (-0.5 * q.astype(np.float64) ** 2 - 0.5 * np.log(2 * np.pi)).sum(-1)
-    r = yf - 1.0 / (1.0 + np.exp(-z))
+    r = yf - np.exp(z - sp)                        # y - sigmoid(z)
     return lp, (r @ Xf - q).astype(np.float32)
 
   q = init.copy() if state is None else state.copy()
@@ -189,6 +190,29 @@ def run_reference(args, w):
               'd2h_bytes_per_step': 0},
   }
   print(json.dumps(line), flush=True)
+
+
+def run_kernel_only(args, w):
+  """Time the batched gradient alone at the full chain batch (profiling aid)."""
+  import torch
+  import probability_gb300 as pg
+  X, y, init = make_data(w)
+  target = pg.LogisticRegression(X, y, precision=args.precision or w['precision'])
+  q = torch.from_numpy(init).cuda()
+  for _ in range(args.warmup):
+    target.log_prob_and_grad(q)
+  torch.cuda.synchronize()
+  e0 = torch.cuda.Event(enable_timing=True)
+  e1 = torch.cuda.Event(enable_timing=True)
+  e0.record()
+  for _ in range(args.steps):
+    target.log_prob_and_grad(q)
+  e1.record()
+  e1.synchronize()
+  ms = e0.elapsed_time(e1) / args.steps
+  flops, nbytes = target.cost(q.shape[0])
+  print(json.dumps({'kernel_only': True, 'precision': target.precision, 'ms_per_eval': ms,
+                    'tflops': flops / ms / 1e9, 'chains': q.shape[0]}), flush=True)
 
 
 def run_engine(args, w):
@@ -274,8 +298,11 @@ def run_engine(args, w):
     grad_evals = int(ge.item())
   value = grad_evals / secs
   draws_t = torch.stack(draws)
-  ess = pg.mcmc.effective_sample_size(draws_t, filter_beyond_positive_pairs=True).sum(0)
-  min_ess_per_s = float(ess.min().item()) / secs if args.steps >= 8 else None
+  min_ess_per_s = None
+  if args.steps >= 20:   # cross-chain ESS (diagnostic.py:220-275) over the timed draws
+    ess = pg.mcmc.effective_sample_size(draws_t, filter_beyond_positive_pairs=True,
+                                        cross_chain_dims=1)
+    min_ess_per_s = float(ess.min().item()) / secs
 
   # ---- roofline of the dominant kernel (batched gradient) ----
   flops_per_grad, bytes_per_batch = target.cost(1)
@@ -338,13 +365,15 @@ def run_engine(args, w):
   cpu = None
   if rank == 0 and world == 1 and not args.no_cpu_baseline:
     budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '20'))
+    sub = 64
     rate, nsteps, dt = cpu_baseline_run(w, X, y, init, budget, 1000000,
-                                        state=state.cpu().numpy(),
+                                        state=state[:sub].cpu().numpy(),
                                         step_size=float(kr.new_step_size.reshape(-1)[0].item()))
     cpu = {'value': rate, 'unit': 'grad-evals/s', 'cores': os.cpu_count(), 'kind': 'port',
-           'sample': '%d DA(NUTS) transitions of all %d chains from the engine\'s adapted '
-                     'state (%.1f s), NumPy float32 oracle, BLAS threads = all cores'
-                     % (nsteps, w['chains'], dt)}
+           'sample': '%d DA(NUTS) transitions of %d of the %d chains, started from the '
+                     'engine\'s adapted state and step size (%.1f s); NumPy float32 oracle, '
+                     'chains in lock-step as in the reference, BLAS threads = all cores'
+                     % (nsteps, sub, w['chains'], dt)}
 
   if rank == 0:
     line = {
@@ -387,10 +416,14 @@ def main():
   ap.add_argument('--workload', default='nuts_logreg_1e5x100', choices=sorted(WORKLOADS))
   ap.add_argument('--precision', default=None, choices=[None, 'fp32', 'mixed'])
   ap.add_argument('--no-cpu-baseline', action='store_true')
+  ap.add_argument('--kernel-only', action='store_true',
+                  help='time the batched log-prob+gradient alone (profiling aid)')
   args = ap.parse_args()
   w = WORKLOADS[args.workload]
   if args.impl == 'reference':
     run_reference(args, w)
+  elif args.kernel_only:
+    run_kernel_only(args, w)
   else:
     run_engine(args, w)
 
