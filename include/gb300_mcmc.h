@@ -92,6 +92,30 @@ GBM_API int gbm_target_dim(const gbm_target* target, int64_t* dim);
 GBM_API int gbm_target_log_prob_and_grad(gbm_target* target, const float* state, int64_t chains,
                                  double* log_prob, float* grad);
 
+/* Allocation-free logistic-regression log-density and gradient.  No
+ * counterpart in the reference: it serves callers that cannot allocate
+ * device memory -- framework custom-call/custom-op slots that hand in only
+ * their own input and output buffers, and serving loops that must not
+ * synchronise the device through cudaMalloc/cudaFree.  Same results as
+ * gbm_target_log_prob_and_grad on a GBM_PRECISION_F32 target, but X [N][D]
+ * float32 and y [N] are the caller's device buffers (no copy, no handle) and
+ * the scratch is a fixed 8 MiB device array inside this library, held on
+ * every GPU that loads it until the process exits.  Runs on the current
+ * device, asynchronously on cuda_stream (NULL = default stream).
+ * Limits: 1 <= num_features <= 256; chains <= 64 * min(2 * SMs,
+ * floor((8 MiB - 256) / (64 * (8 + 4 * num_features)))) -- 19456 chains at
+ * 100 features on GB300; larger requests fail with GBM_EINVAL.  The first
+ * call on a device resolves the scratch array's device address
+ * (cudaGetSymbolAddress) and sets kernel attributes; make that first call
+ * before any stream capture.  Calls share the one scratch array: calls that
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  Allocates nothing. */
+GBM_API int gbm_logreg_log_prob_and_grad_noalloc(const float* x, int64_t num_rows,
+                                                 int64_t num_features, const float* y,
+                                                 float prior_scale, const float* state,
+                                                 int64_t chains, double* log_prob, float* grad,
+                                                 void* cuda_stream);
+
 /* Algorithmic flops and HBM bytes of one batched evaluation at `chains`. */
 GBM_API int gbm_target_cost(const gbm_target* target, int64_t chains, double* flops, double* bytes);
 

@@ -58,6 +58,8 @@ _SIGNATURES = {
     'gbm_dual_averaging_update': (
         [P, I64, P, ctypes.c_int, I32, F64, P, F64, F64, F64, P, P], ctypes.c_int),
     'gbm_step_key': ([U32P, ctypes.c_uint64, U32P], ctypes.c_int),
+    'gbm_logreg_log_prob_and_grad_noalloc': ([P, I64, I64, P, F32, P, I64, P, P, P],
+                                             ctypes.c_int),
 }
 
 

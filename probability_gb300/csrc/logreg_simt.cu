@@ -24,7 +24,6 @@
 #include "engine.h"
 
 namespace gbm {
-namespace {
 
 constexpr int kCT = 64;        // chains per tile
 constexpr int kNT = 64;        // data rows per tile
@@ -272,7 +271,9 @@ class LogregSimt final : public Target {
   DeviceBuffer x_, y_;
 };
 
-}  // namespace
+namespace {
+
+} // namespace
 
 std::unique_ptr<Target> make_logreg_simt(gbm_context* ctx, const float* X, int64_t n, int64_t d,
                                          const float* y, float prior_scale) {
@@ -281,3 +282,165 @@ std::unique_ptr<Target> make_logreg_simt(gbm_context* ctx, const float* X, int64
 }
 
 }  // namespace gbm
+
+// ---------------------------------------------------------------------------
+// Allocation-free logistic-regression log-density + gradient.
+//
+// Some callers cannot allocate device memory at all: code embedded in a host
+// framework's custom-call or custom-op slot, which receives only the input
+// and output buffers the framework owns and must not grow its own pool, and
+// latency-bound serving loops that cannot afford the device-wide
+// synchronisation cudaMalloc/cudaFree can cause.  For them this entry point
+// keeps the kernel's scratch (the per-split partial log-likelihoods and
+// gradients, and the batch-size word) in a fixed file-scope device array
+// instead of a workspace.  The array occupies kNoAllocScratchBytes on every
+// GPU that loads this library, for the life of the process.
+// ---------------------------------------------------------------------------
+#include <cstdio>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "gb300_mcmc.h"
+
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = 8u << 20;  // 8 MiB per device
+constexpr size_t kNoAllocCountBytes = 256;          // batch-size word, padded
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+__global__ void noalloc_set_count(int* count, int n) { *count = n; }
+
+struct NoAllocDevice {
+  bool ready = false;
+  unsigned char* scratch = nullptr;  // device address of g_noalloc_scratch
+  int num_sms = 0;
+};
+
+std::mutex g_noalloc_mu;
+std::vector<NoAllocDevice> g_noalloc_devices;
+
+// Once per device, with that device current: resolve the device address of
+// the scratch array (its host-side name is only a stand-in) and raise the
+// kernels' dynamic shared-memory limit.  Allocates nothing.
+int noalloc_setup(int device, NoAllocDevice** out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mu);
+  if ((int)g_noalloc_devices.size() <= device) g_noalloc_devices.resize(device + 1);
+  NoAllocDevice& d = g_noalloc_devices[device];
+  if (!d.ready) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess) {
+      gbm::set_error(std::string("cudaGetSymbolAddress(g_noalloc_scratch): ") +
+                     cudaGetErrorString(e));
+      return GBM_ECUDA;
+    }
+    e = cudaDeviceGetAttribute(&d.num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e != cudaSuccess) {
+      gbm::set_error(std::string("cudaDeviceGetAttribute: ") + cudaGetErrorString(e));
+      return GBM_ECUDA;
+    }
+    const int kds[4] = {2, 4, 8, 16};
+    for (int kd : kds) {
+      const size_t smem = sizeof(float) * (size_t)(kd * 16) * (gbm::kCT + gbm::kXPad) +
+                          sizeof(float) * gbm::kNT * gbm::kCT;
+      const void* fn = kd == 2 ? (const void*)gbm::logreg_partial_kernel<2>
+                     : kd == 4 ? (const void*)gbm::logreg_partial_kernel<4>
+                     : kd == 8 ? (const void*)gbm::logreg_partial_kernel<8>
+                               : (const void*)gbm::logreg_partial_kernel<16>;
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+      if (e != cudaSuccess) {
+        gbm::set_error(std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e));
+        return GBM_ECUDA;
+      }
+    }
+    d.scratch = static_cast<unsigned char*>(p);
+    d.ready = true;
+  }
+  *out = &d;
+  return GBM_OK;
+}
+
+}  // namespace
+
+extern "C" int gbm_logreg_log_prob_and_grad_noalloc(const float* x, int64_t num_rows,
+                                                    int64_t num_features, const float* y,
+                                                    float prior_scale, const float* state,
+                                                    int64_t chains, double* log_prob,
+                                                    float* grad, void* cuda_stream) {
+  if (!x || !y || !state || !log_prob || !grad) {
+    gbm::set_error("gbm_logreg_log_prob_and_grad_noalloc: NULL argument");
+    return GBM_EINVAL;
+  }
+  if (num_rows <= 0 || num_rows >= ((int64_t)1 << 31) || chains <= 0) {
+    gbm::set_error("gbm_logreg_log_prob_and_grad_noalloc: need 0 < num_rows < 2^31, chains > 0");
+    return GBM_EINVAL;
+  }
+  if (num_features <= 0 || num_features > 256) {
+    gbm::set_error("gbm_logreg_log_prob_and_grad_noalloc: num_features must be in [1, 256]");
+    return GBM_EINVAL;
+  }
+  if (!(prior_scale > 0.f)) {
+    gbm::set_error("gbm_logreg_log_prob_and_grad_noalloc: prior_scale must be > 0");
+    return GBM_EINVAL;
+  }
+  int device = 0;
+  cudaError_t e = cudaGetDevice(&device);
+  if (e != cudaSuccess) {
+    gbm::set_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    return GBM_ECUDA;
+  }
+  NoAllocDevice* dev = nullptr;
+  int st = noalloc_setup(device, &dev);
+  if (st != GBM_OK) return st;
+
+  // Scratch layout: [count word | lpart: rows doubles | gpart: rows * D floats],
+  // rows = grid * kCT >= S * chains.  The grid shrinks as D grows so the
+  // partials fit; chains is then limited to grid * kCT.
+  const int D = (int)num_features, N = (int)num_rows;
+  const size_t per_row = sizeof(double) + sizeof(float) * (size_t)D;
+  const size_t avail = kNoAllocScratchBytes - kNoAllocCountBytes;
+  int grid = 2 * dev->num_sms;
+  const int fit = (int)(avail / (per_row * gbm::kCT));
+  grid = std::min(grid, fit);
+  if (grid < 1 || chains > (int64_t)grid * gbm::kCT) {
+    char msg[256];
+    snprintf(msg, sizeof(msg),
+             "gbm_logreg_log_prob_and_grad_noalloc: %lld chains exceed the fixed %zu-byte "
+             "scratch at %d features (maximum %d chains)",
+             (long long)chains, kNoAllocScratchBytes, D, std::max(grid, 0) * gbm::kCT);
+    gbm::set_error(msg);
+    return GBM_EINVAL;
+  }
+  const int n = (int)chains;
+  int* count = reinterpret_cast<int*>(dev->scratch);
+  double* lpart = reinterpret_cast<double*>(dev->scratch + kNoAllocCountBytes);
+  float* gpart = reinterpret_cast<float*>(lpart + (size_t)grid * gbm::kCT);
+  cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
+  const int kd = D <= 32 ? 2 : D <= 64 ? 4 : D <= 128 ? 8 : 16;
+  const size_t smem = sizeof(float) * (size_t)(kd * 16) * (gbm::kCT + gbm::kXPad) +
+                      sizeof(float) * gbm::kNT * gbm::kCT;
+  const float inv_var = 1.f / (prior_scale * prior_scale);
+  const double log_norm = -log((double)prior_scale) - 0.5 * log(2.0 * M_PI);
+  noalloc_set_count<<<1, 1, 0, s>>>(count, n);
+  switch (kd) {
+    case 2: gbm::logreg_partial_kernel<2><<<grid, gbm::kThreads, smem, s>>>(
+        x, D, y, N, D, state, D, count, grid, lpart, gpart); break;
+    case 4: gbm::logreg_partial_kernel<4><<<grid, gbm::kThreads, smem, s>>>(
+        x, D, y, N, D, state, D, count, grid, lpart, gpart); break;
+    case 8: gbm::logreg_partial_kernel<8><<<grid, gbm::kThreads, smem, s>>>(
+        x, D, y, N, D, state, D, count, grid, lpart, gpart); break;
+    default: gbm::logreg_partial_kernel<16><<<grid, gbm::kThreads, smem, s>>>(
+        x, D, y, N, D, state, D, count, grid, lpart, gpart); break;
+  }
+  gbm::logreg_reduce_kernel<<<(n + 7) / 8, 256, 0, s>>>(lpart, gpart, state, D, count, grid, N,
+                                                         D, inv_var, log_norm, log_prob, grad, D);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    gbm::set_error(std::string("gbm_logreg_log_prob_and_grad_noalloc launch: ") +
+                   cudaGetErrorString(e));
+    return GBM_ECUDA;
+  }
+  return GBM_OK;
+}
