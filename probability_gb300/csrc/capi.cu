@@ -33,6 +33,10 @@ int guarded(F&& f) {
   } catch (const gbm::CudaError& e) {
     set_error(std::string(e.what) + ": " + cudaGetErrorString(e.err));
     return e.err == cudaErrorMemoryAllocation ? GBM_ENOMEM : GBM_ECUDA;
+  } catch (const gbm::DeviceTimeout& e) {
+    set_error("a bounded device wait timed out inside a kernel (code " +
+              std::to_string(e.code) + ")");
+    return GBM_ETIMEDOUT;
   } catch (const std::bad_alloc&) {
     set_error("host allocation failed");
     return GBM_ENOMEM;
@@ -200,6 +204,8 @@ int gbm_target_log_prob_and_grad(gbm_target* t, const float* state, int64_t chai
     // The count word is host memory of this frame; finish the copy before
     // returning.
     GBM_CUDA(cudaStreamSynchronize(s));
+    const int e = t->impl->device_error(s);
+    if (e) throw gbm::DeviceTimeout{e};
     return GBM_OK;
   });
 }

@@ -25,6 +25,11 @@ struct CudaError {
   const char* what;
 };
 
+// A kernel's bounded device wait ran out; `code` says which wait.
+struct DeviceTimeout {
+  int code;
+};
+
 #define GBM_CUDA(call)                                                     \
   do {                                                                     \
     cudaError_t _e = (call);                                               \

@@ -56,6 +56,9 @@ struct Target {
   virtual double bytes(int64_t n) const = 0;
   // Kernels one eval() launches (for launch accounting).
   virtual int launches_per_eval() const = 0;
+  // Error word written by kernels whose bounded device waits ran out
+  // (0 = none).  Synchronizes `s`.
+  virtual int device_error(cudaStream_t s) { (void)s; return 0; }
 };
 
 std::unique_ptr<Target> make_logreg_simt(gbm_context* ctx, const float* X, int64_t n,

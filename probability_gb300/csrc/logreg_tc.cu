@@ -1,9 +1,479 @@
-// Mixed-precision (tcgen05) logistic-regression target: not built yet.
+// Mixed-precision fused logistic-regression log-density + gradient on the
+// 5th-generation tensor cores (tcgen05, TMEM accumulators, TMA).
+//
+// Same mathematics as logreg_simt.cu (the inference_gym logistic-regression
+// target, spinoffs/inference_gym/inference_gym/targets/logistic_regression.py:
+// 92-103; distributions/bernoulli.py:126-140), computed as
+//   Z  = X_tile  B^T          (M = 128 rows, N = chain tile, K = features)
+//   R  = y - sigmoid(Z),  logp += sum_rows log Bernoulli(y | Z)
+//   G += X_tile^T R           (M = 128 features, N = chain tile, K = 128 rows)
+// with BF16 operands and FP32 accumulation.  X is stored as BF16; the FP32
+// chain states B and residuals R are each split into a BF16 high part and a
+// BF16 residual (hi + lo), and both parts are multiplied (residual
+// correction), so Z and G carry ~16 significant bits of the FP32 operands.
+//
+// One X tile in shared memory (TMA, 128-byte swizzle, [64-feature block]
+// [128 rows][128 B]) is read by both MMAs: as the K-major A operand of the
+// first and, unchanged, as the MN-major A operand (X^T) of the second.  X is
+// therefore read from HBM/L2 once per chain tile.  Z and G live in TMEM.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <memory>
+#include <string>
+
 #include "engine.h"
+#include "tc_ptx.cuh"
 
 namespace gbm {
-std::unique_ptr<Target> make_logreg_tc(gbm_context*, const void*, int, int64_t, int64_t,
-                                       const float*, float) {
-  return nullptr;
+namespace {
+
+constexpr int kRows = 128;               // rows of X per tile (MMA M of GEMM1)
+constexpr int kThreadsTc = 128;          // 4 warps: one per TMEM lane quarter
+constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s bound on every device wait
+constexpr uint32_t kTmemCols = 256;
+
+enum TcError : int { kTcOk = 0, kTcTimeoutTma = 1, kTcTimeoutMma1 = 2, kTcTimeoutMma2 = 3 };
+
+__host__ __device__ inline int tc_splits(int n, int ct, int grid, int row_tiles) {
+  const int tiles = (n + ct - 1) / ct;
+  if (tiles == 0) return 0;
+  int s = grid / tiles;
+  s = s < 1 ? 1 : s;
+  return s > row_tiles ? row_tiles : s;
 }
+
+template <int KB, int CT>
+struct TcLayout {
+  static constexpr int kXBytes = KB * 16384;           // [KB][128 rows][128 B]
+  static constexpr int kBBytes = KB * CT * 128;        // [KB][CT rows][128 B]
+  static constexpr int kRBytes = (CT / 64) * 16384;    // [CT/64][128 rows][128 B]
+  static constexpr int kX = 0;
+  static constexpr int kBhi = kX + kXBytes;
+  static constexpr int kBlo = kBhi + kBBytes;
+  static constexpr int kRhi = kBlo + kBBytes;
+  static constexpr int kRlo = kRhi + kRBytes;
+  static constexpr int kCtl = kRlo + kRBytes;          // barriers, flags
+  static constexpr int kRed = kCtl + 64;               // [4 warps][CT] doubles
+  static constexpr int kBytes = kRed + 4 * CT * 8;
+  static constexpr int kMTiles = KB / 2;               // 128-feature tiles of G
+};
+
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
+  return *reinterpret_cast<uint32_t*>(&v);
+}
+
+template <int KB, int CT>
+__global__ void __launch_bounds__(kThreadsTc, 1)
+logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restrict__ y, int N,
+                 int D, const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev,
+                 int grid, double* __restrict__ lpart, float* __restrict__ gpart,
+                 int* __restrict__ err) {
+  using L = TcLayout<KB, CT>;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  // Dynamic shared memory is only guaranteed 16-byte aligned: round up.
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int n = *n_dev;
+  const int row_tiles = (N + kRows - 1) / kRows;
+  const int S = tc_splits(n, CT, grid, row_tiles);
+  const int tiles = (n + CT - 1) / CT;
+  if (S == 0 || (int)blockIdx.x >= tiles * S) return;
+  const int tile = blockIdx.x % tiles, split = blockIdx.x / tiles;
+  const int c0 = tile * CT;
+  const int rt_begin = (int)((long long)split * row_tiles / S);
+  const int rt_end = (int)((long long)(split + 1) * row_tiles / S);
+
+  unsigned char* Xs = smem + L::kX;
+  unsigned char* Bhi = smem + L::kBhi;
+  unsigned char* Blo = smem + L::kBlo;
+  unsigned char* Rhi = smem + L::kRhi;
+  unsigned char* Rlo = smem + L::kRlo;
+  uint64_t* bar_x = reinterpret_cast<uint64_t*>(smem + L::kCtl);
+  uint64_t* bar_z = bar_x + 1;
+  uint64_t* bar_g = bar_x + 2;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_x + 3);
+  double* red = reinterpret_cast<double*>(smem + L::kRed);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    tc::mbar_init(bar_x, 1);
+    tc::mbar_init(bar_z, 1);
+    tc::mbar_init(bar_g, 1);
+    tc::fence_mbar_init();
+    tc::prefetch_tmap(&xmap);
+  }
+  if (warp == 0) tc::tmem_alloc(tmem_slot, kTmemCols);
+
+  // Chain states -> BF16 hi/lo, K-major 128-byte-swizzled [KB][CT][128 B].
+  for (int i = tid; i < CT * KB * 8; i += kThreadsTc) {
+    const int c = i / (KB * 8), chunk = i % (KB * 8);
+    const int d0 = chunk * 8;
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int d = d0 + e;
+      v[e] = (c0 + c < n && d < D) ? Q[(size_t)(c0 + c) * ldq + d] : 0.f;
+    }
+    uint32_t hi[4], lo[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * e], v[2 * e + 1]);
+      hi[e] = *reinterpret_cast<const uint32_t*>(&h);
+      const float2 hf = __bfloat1622float2(h);
+      lo[e] = pack_bf16x2(v[2 * e] - hf.x, v[2 * e + 1] - hf.y);
+    }
+    const int kb = d0 >> 6;
+    const uint32_t off = kb * (CT * 128) + tc::sw128_offset(c, d0 & 63);
+    *reinterpret_cast<uint4*>(Bhi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+    *reinterpret_cast<uint4*>(Blo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+  }
+  tc::fence_proxy_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+  const uint32_t tz = tmem;               // Z: columns [0, CT)
+  const uint32_t tg = tmem + CT;          // G: columns [CT, CT * (1 + KB/2))
+  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
+
+  constexpr uint32_t idesc1 = tc::idesc_bf16_f32(128, CT, false, false);  // K-major A, B
+  constexpr uint32_t idesc2 = tc::idesc_bf16_f32(128, CT, true, true);    // MN-major A, B
+  const uint32_t xs_a = tc::smem_u32(Xs), bhi_a = tc::smem_u32(Bhi), blo_a = tc::smem_u32(Blo);
+  const uint32_t rhi_a = tc::smem_u32(Rhi), rlo_a = tc::smem_u32(Rlo);
+
+  float lp_acc[CT];
+#pragma unroll
+  for (int c = 0; c < CT; ++c) lp_acc[c] = 0.f;
+
+  bool ok = true;
+  int it = 0;
+  for (int rt = rt_begin; rt < rt_end && ok; ++rt, ++it) {
+    const uint32_t ph = it & 1;
+    if (tid == 0) {
+      tc::mbar_arrive_expect_tx(bar_x, L::kXBytes);
+#pragma unroll
+      for (int kb = 0; kb < KB; ++kb)
+        tc::tma_load_2d(Xs + kb * 16384, &xmap, kb * 64, rt * kRows, bar_x);
+    }
+    ok = tc::mbar_wait(bar_x, ph, kWaitLimitNs);
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0) atomicExch(err, kTcTimeoutTma);
+      ok = false;
+      break;
+    }
+    // GEMM1: Z = X B^T (B = hi + lo).
+    if (tid == 0) {
+      tc::tc_fence_after();
+#pragma unroll
+      for (int kb = 0; kb < KB; ++kb) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+          const uint64_t a = tc::smem_desc_sw128(xs_a + kb * 16384 + k * 32, 16, 1024);
+          const uint64_t bh = tc::smem_desc_sw128(bhi_a + kb * (CT * 128) + k * 32, 16, 1024);
+          const uint64_t bl = tc::smem_desc_sw128(blo_a + kb * (CT * 128) + k * 32, 16, 1024);
+          tc::mma_bf16(tz, a, bh, idesc1, (kb | k) ? 1u : 0u);
+          tc::mma_bf16(tz, a, bl, idesc1, 1u);
+        }
+      }
+      tc::mma_commit(bar_z);
+    }
+    ok = tc::mbar_wait(bar_z, ph, kWaitLimitNs);
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0) atomicExch(err, kTcTimeoutMma1);
+      ok = false;
+      break;
+    }
+    tc::tc_fence_after();
+    // Epilogue: thread owns row r = 32 * warp + lane of the tile.
+    const int r = warp * 32 + lane;
+    const int row = rt * kRows + r;
+    const bool valid = row < N;
+    const float yv = valid ? y[row] : 0.f;
+#pragma unroll
+    for (int ch = 0; ch < CT / 16; ++ch) {
+      float z[16];
+      tc::tmem_ld16(tz + lane_base + ch * 16, z);
+      tc::tmem_ld_wait();
+      float rv[16];
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        const float zz = z[j];
+        // bernoulli.py:126-140: -softplus(z)(1-y) - softplus(-z) y
+        const float t = __expf(-fabsf(zz));
+        const float l1p = log1pf(t);
+        const float sp_pos = fmaxf(zz, 0.f) + l1p;   // softplus(z)
+        const float sp_neg = sp_pos - zz;            // softplus(-z)
+        const float lp = -sp_pos * (1.f - yv) - sp_neg * yv;
+        const float inv = __frcp_rn(1.f + t);
+        const float sig = zz >= 0.f ? inv : t * inv;
+        lp_acc[ch * 16 + j] += valid ? lp : 0.f;
+        rv[j] = valid ? (yv - sig) : 0.f;
+      }
+      // R tile, MN-major (chains contiguous), [CT/64][128 rows][128 B].
+#pragma unroll
+      for (int half = 0; half < 2; ++half) {
+        const int c = ch * 16 + half * 8;
+        uint32_t hi[4], lo[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float a = rv[half * 8 + 2 * e], b = rv[half * 8 + 2 * e + 1];
+          const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
+          hi[e] = *reinterpret_cast<const uint32_t*>(&h);
+          const float2 hf = __bfloat1622float2(h);
+          lo[e] = pack_bf16x2(a - hf.x, b - hf.y);
+        }
+        const uint32_t off = (c >> 6) * 16384 + tc::sw128_offset(r, c & 63);
+        *reinterpret_cast<uint4*>(Rhi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+        *reinterpret_cast<uint4*>(Rlo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+      }
+    }
+    tc::fence_proxy_async_smem();
+    tc::tc_fence_before();
+    __syncthreads();
+    // GEMM2: G += X^T R (R = hi + lo), per 128-feature tile of G.
+    if (tid == 0) {
+      tc::tc_fence_after();
+#pragma unroll
+      for (int mt = 0; mt < L::kMTiles; ++mt) {
+#pragma unroll
+        for (int ks = 0; ks < kRows / 16; ++ks) {
+          const uint64_t a = tc::smem_desc_sw128(xs_a + mt * 2 * 16384 + ks * 2048, 16384, 1024);
+          const uint64_t bh = tc::smem_desc_sw128(rhi_a + ks * 2048, 16384, 1024);
+          const uint64_t bl = tc::smem_desc_sw128(rlo_a + ks * 2048, 16384, 1024);
+          tc::mma_bf16(tg + mt * CT, a, bh, idesc2, (it > 0 || ks > 0) ? 1u : 0u);
+          tc::mma_bf16(tg + mt * CT, a, bl, idesc2, 1u);
+        }
+      }
+      tc::mma_commit(bar_g);
+    }
+    ok = tc::mbar_wait(bar_g, ph, kWaitLimitNs);
+    if (!__syncthreads_and(ok)) {
+      if (tid == 0) atomicExch(err, kTcTimeoutMma2);
+      ok = false;
+      break;
+    }
+  }
+
+  if (ok) {
+    tc::tc_fence_after();
+    // Gradient partials: TMEM lane = feature, column = chain.
+    if (it > 0) {
+#pragma unroll
+      for (int mt = 0; mt < L::kMTiles; ++mt) {
+        const int d = mt * 128 + warp * 32 + lane;
+#pragma unroll
+        for (int ch = 0; ch < CT / 16; ++ch) {
+          float g[16];
+          tc::tmem_ld16(tg + mt * CT + lane_base + ch * 16, g);
+          tc::tmem_ld_wait();
+          if (d < D) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int c = c0 + ch * 16 + j;
+              if (c < n) gpart[((size_t)split * n + c) * D + d] = g[j];
+            }
+          }
+        }
+      }
+    } else {
+      for (int i = tid; i < CT * D; i += kThreadsTc) {
+        const int c = c0 + i / D;
+        if (c < n) gpart[((size_t)split * n + c) * D + i % D] = 0.f;
+      }
+    }
+    // Log-likelihood partials: sum over the 128 rows (threads) per chain.
+#pragma unroll
+    for (int c = 0; c < CT; ++c) {
+      double v = (double)lp_acc[c];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+      if (lane == 0) red[warp * CT + c] = v;
+    }
+    __syncthreads();
+    for (int c = tid; c < CT; c += kThreadsTc) {
+      const double s = red[c] + red[CT + c] + red[2 * CT + c] + red[3 * CT + c];
+      if (c0 + c < n) lpart[(size_t)split * n + c0 + c] = s;
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+__global__ void tc_reduce_kernel(const double* __restrict__ lpart, const float* __restrict__ gpart,
+                                 const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev,
+                                 int ct, int grid, int N, int D, float inv_var, double log_norm,
+                                 double* __restrict__ logp, float* __restrict__ grad, int ldg) {
+  const int n = *n_dev;
+  const int S = tc_splits(n, ct, grid, (N + kRows - 1) / kRows);
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  if (warp >= n) return;
+  const float* q = Q + (size_t)warp * ldq;
+  double prior = 0.0;
+  for (int d = lane; d < D; d += 32) {
+    const float qd = q[d];
+    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+    int s = 0;
+    for (; s + 4 <= S; s += 4) {
+      a0 += gpart[((size_t)(s + 0) * n + warp) * D + d];
+      a1 += gpart[((size_t)(s + 1) * n + warp) * D + d];
+      a2 += gpart[((size_t)(s + 2) * n + warp) * D + d];
+      a3 += gpart[((size_t)(s + 3) * n + warp) * D + d];
+    }
+    for (; s < S; ++s) a0 += gpart[((size_t)s * n + warp) * D + d];
+    grad[(size_t)warp * ldg + d] = ((a0 + a1) + (a2 + a3)) - qd * inv_var;
+    prior += (double)qd * (double)qd;
+  }
+  prior = warp_sum(prior);
+  if (lane == 0) {
+    double lp = 0.0;
+    for (int s = 0; s < S; ++s) lp += lpart[(size_t)s * n + warp];
+    logp[warp] = lp - 0.5 * (double)inv_var * prior + (double)D * log_norm;
+  }
+}
+
+__global__ void to_bf16_padded(const float* __restrict__ X, int64_t N, int D, int Dp,
+                               __nv_bfloat16* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N * Dp) return;
+  const int64_t r = i / Dp;
+  const int d = (int)(i % Dp);
+  out[i] = __float2bfloat16_rn(d < D ? X[r * D + d] : 0.f);
+}
+
+__global__ void bf16_pad(const __nv_bfloat16* __restrict__ X, int64_t N, int D, int Dp,
+                         __nv_bfloat16* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N * Dp) return;
+  const int64_t r = i / Dp;
+  const int d = (int)(i % Dp);
+  out[i] = d < D ? X[r * D + d] : __float2bfloat16_rn(0.f);
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    GBM_CUDA(cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                              cudaEnableDefault, &q));
+    if (q != cudaDriverEntryPointSuccess || !p)
+      throw CudaError{cudaErrorNotSupported, "cuTensorMapEncodeTiled entry point"};
+    fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+class LogregTc final : public Target {
+ public:
+  LogregTc(gbm_context* ctx, const void* X, int x_dtype, int64_t n, int64_t d, const float* y,
+           float prior_scale)
+      : N_(n), D_(d) {
+    dim = d;
+    kb_ = d <= 128 ? 2 : 4;
+    ct_ = kb_ == 2 ? 128 : 64;
+    const int Dp = kb_ * 64;
+    xb_.reserve(sizeof(__nv_bfloat16) * (size_t)N_ * Dp);
+    y_.reserve(sizeof(float) * (size_t)N_);
+    err_.reserve(256);
+    const int64_t total = N_ * Dp;
+    const int tb = 256;
+    const int64_t blocks = (total + tb - 1) / tb;
+    if (x_dtype == 0)
+      to_bf16_padded<<<(unsigned)blocks, tb, 0, ctx->stream>>>(
+          static_cast<const float*>(X), N_, (int)D_, Dp, xb_.as<__nv_bfloat16>());
+    else
+      bf16_pad<<<(unsigned)blocks, tb, 0, ctx->stream>>>(
+          static_cast<const __nv_bfloat16*>(X), N_, (int)D_, Dp, xb_.as<__nv_bfloat16>());
+    GBM_CUDA(cudaGetLastError());
+    GBM_CUDA(cudaMemcpyAsync(y_.ptr, y, sizeof(float) * N_, cudaMemcpyDeviceToDevice,
+                             ctx->stream));
+    GBM_CUDA(cudaMemsetAsync(err_.ptr, 0, 256, ctx->stream));
+    inv_var_ = 1.f / (prior_scale * prior_scale);
+    log_norm_ = -log((double)prior_scale) - 0.5 * log(2.0 * M_PI);
+    grid_ = ctx->num_sms;
+    // Tensor map over X_bf16 [N][Dp]: boxes of 64 features x 128 rows,
+    // 128-byte swizzle, rows past N read as zeros.
+    cuuint64_t dims[2] = {(cuuint64_t)Dp, (cuuint64_t)N_};
+    cuuint64_t strides[1] = {(cuuint64_t)Dp * 2};
+    cuuint32_t box[2] = {64, (cuuint32_t)kRows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode_tiled()(&xmap_, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, xb_.ptr, dims,
+                                strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw CudaError{cudaErrorInvalidValue, "cuTensorMapEncodeTiled"};
+    smem_ = (kb_ == 2 ? TcLayout<2, 128>::kBytes : TcLayout<4, 64>::kBytes) + 1024;
+    if (kb_ == 2)
+      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<2, 128>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_));
+    else
+      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<4, 64>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_));
+  }
+
+  size_t workspace_bytes(int64_t cap) const override {
+    const size_t rows = (size_t)grid_ * ct_ + (size_t)cap;
+    return rows * sizeof(double) + rows * (size_t)D_ * sizeof(float) + 256;
+  }
+
+  void eval(const float* q, int ldq, const int* n_dev, int cap, double* logp, float* grad,
+            int ldg, void* ws, cudaStream_t s) override {
+    const size_t rows = (size_t)grid_ * ct_ + (size_t)cap;
+    double* lpart = static_cast<double*>(ws);
+    float* gpart = reinterpret_cast<float*>(lpart + rows);
+    const int N = (int)N_, D = (int)D_;
+    if (kb_ == 2)
+      logreg_tc_kernel<2, 128><<<grid_, kThreadsTc, smem_, s>>>(
+          xmap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_.as<int>());
+    else
+      logreg_tc_kernel<4, 64><<<grid_, kThreadsTc, smem_, s>>>(
+          xmap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_.as<int>());
+    GBM_CUDA(cudaGetLastError());
+    tc_reduce_kernel<<<(cap + 7) / 8, 256, 0, s>>>(lpart, gpart, q, ldq, n_dev, ct_, grid_, N, D,
+                                                   inv_var_, log_norm_, logp, grad, ldg);
+    GBM_CUDA(cudaGetLastError());
+  }
+
+  int device_error(cudaStream_t s) override {
+    int e = 0;
+    GBM_CUDA(cudaMemcpyAsync(&e, err_.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
+    GBM_CUDA(cudaStreamSynchronize(s));
+    return e;
+  }
+
+  int launches_per_eval() const override { return 2; }
+  double flops(int64_t n) const override { return 4.0 * (double)N_ * D_ * n; }
+  double bytes(int64_t n) const override {
+    return 2.0 * (double)N_ * D_ + 4.0 * N_ + 8.0 * (double)n * D_ + 8.0 * n;
+  }
+
+ private:
+  int64_t N_, D_;
+  int kb_ = 2, ct_ = 128, grid_ = 0;
+  size_t smem_ = 0;
+  float inv_var_ = 1.f;
+  double log_norm_ = 0.0;
+  DeviceBuffer xb_, y_, err_;
+  CUtensorMap xmap_;
+};
+
+}  // namespace
+
+std::unique_ptr<Target> make_logreg_tc(gbm_context* ctx, const void* X, int x_dtype, int64_t n,
+                                       int64_t d, const float* y, float prior_scale) {
+  if (d > 256) return nullptr;
+  return std::unique_ptr<Target>(new LogregTc(ctx, X, x_dtype, n, d, y, prior_scale));
+}
+
 }  // namespace gbm

@@ -607,6 +607,8 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
       GBM_CUDA(cudaMemcpyAsync(host_flags, w.any_cont, sizeof(int), cudaMemcpyDeviceToHost, s));
       GBM_CUDA(cudaStreamSynchronize(s));
       if (k->profiling) nuts_profile_flush(k);
+      const int dev_err = k->target->impl->device_error(s);
+      if (dev_err) throw DeviceTimeout{dev_err};
       if (host_flags[0] == 0) break;
     }
     nuts_depth_begin_kernel<<<(int)((chains + tb - 1) / tb), tb, 0, s>>>(w, key, depth);
