@@ -3,19 +3,31 @@
 //
 // Same mathematics as logreg_simt.cu (the inference_gym logistic-regression
 // target, spinoffs/inference_gym/inference_gym/targets/logistic_regression.py:
-// 92-103; distributions/bernoulli.py:126-140), computed as
-//   Z  = X_tile  B^T          (M = 128 rows, N = chain tile, K = features)
+// 92-103; distributions/bernoulli.py:126-140), computed per 128-row tile as
+//   Z  = X_tile B^T          (M = 128 rows, N = chain tile, K = features)
 //   R  = y - sigmoid(Z),  logp += sum_rows log Bernoulli(y | Z)
-//   G += X_tile^T R           (M = 128 features, N = chain tile, K = 128 rows)
-// with BF16 operands and FP32 accumulation.  X is stored as BF16; the FP32
-// chain states B and residuals R are each split into a BF16 high part and a
-// BF16 residual (hi + lo), and both parts are multiplied (residual
-// correction), so Z and G carry ~16 significant bits of the FP32 operands.
+//   G += X_tile^T R          (M = 128 features, N = chain tile, K = 128 rows)
+// with BF16 operands and FP32 accumulation in TMEM.  X is BF16; the FP32
+// chain states B are split into a BF16 high part and a BF16 residual and
+// both are multiplied (residual correction), so Z -- and therefore the
+// log-density that drives acceptance -- carries ~16 significant bits of the
+// states.  R enters the gradient contraction as BF16.  A gradient that is a
+// deterministic function of the state keeps the leapfrog map reversible and
+// volume-preserving, so the sampler stays exact; only its acceptance rate
+// depends on the gradient's accuracy.
 //
 // One X tile in shared memory (TMA, 128-byte swizzle, [64-feature block]
 // [128 rows][128 B]) is read by both MMAs: as the K-major A operand of the
-// first and, unchanged, as the MN-major A operand (X^T) of the second.  X is
-// therefore read from HBM/L2 once per chain tile.  Z and G live in TMEM.
+// first and, unchanged, as the MN-major A operand (X^T) of the second, so X is
+// read from HBM/L2 once per chain tile.
+//
+// Warp roles (320 threads): warp 0 issues TMA loads, warp 1 allocates TMEM
+// and issues the MMAs, warps 2-9 run the epilogue (two warps per TMEM lane
+// quarter, each on half of the chain tile).  X stages, Z accumulators and R
+// tiles are double-buffered, so GEMM1 of tile i+1 and GEMM2 of tile i run on
+// the tensor core while the epilogue works on tile i+1.  Every wait is
+// bounded (%globaltimer); on timeout the kernel records an error code, drains
+// what it issued and frees its TMEM.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -30,12 +42,17 @@
 namespace gbm {
 namespace {
 
-constexpr int kRows = 128;               // rows of X per tile (MMA M of GEMM1)
-constexpr int kThreadsTc = 128;          // 4 warps: one per TMEM lane quarter
-constexpr uint64_t kWaitLimitNs = 2000000000ull;  // 2 s bound on every device wait
-constexpr uint32_t kTmemCols = 256;
+constexpr int kRows = 128;                         // rows of X per tile
+constexpr int kEpiWarps = 8;
+constexpr int kThreadsTc = 32 * (2 + kEpiWarps);   // 320
+constexpr uint64_t kWaitLimitNs = 2000000000ull;   // 2 s bound on every device wait
 
-enum TcError : int { kTcOk = 0, kTcTimeoutTma = 1, kTcTimeoutMma1 = 2, kTcTimeoutMma2 = 3 };
+enum TcError : int {
+  kTcOk = 0,
+  kTcTimeoutTma = 1,
+  kTcTimeoutMma = 2,
+  kTcTimeoutEpilogue = 3,
+};
 
 __host__ __device__ inline int tc_splits(int n, int ct, int grid, int row_tiles) {
   const int tiles = (n + ct - 1) / ct;
@@ -47,23 +64,47 @@ __host__ __device__ inline int tc_splits(int n, int ct, int grid, int row_tiles)
 
 template <int KB, int CT>
 struct TcLayout {
-  static constexpr int kXBytes = KB * 16384;           // [KB][128 rows][128 B]
+  static constexpr int kXStage = KB * 16384;           // [KB][128 rows][128 B]
   static constexpr int kBBytes = KB * CT * 128;        // [KB][CT rows][128 B]
-  static constexpr int kRBytes = (CT / 64) * 16384;    // [CT/64][128 rows][128 B]
-  static constexpr int kX = 0;
-  static constexpr int kBhi = kX + kXBytes;
+  static constexpr int kRBuf = (CT / 64) * 16384;      // [CT/64][128 rows][128 B]
+  static constexpr int kX = 0;                         // 2 stages
+  static constexpr int kBhi = kX + 2 * kXStage;
   static constexpr int kBlo = kBhi + kBBytes;
-  static constexpr int kRhi = kBlo + kBBytes;
-  static constexpr int kRlo = kRhi + kRBytes;
-  static constexpr int kCtl = kRlo + kRBytes;          // barriers, flags
-  static constexpr int kRed = kCtl + 64;               // [4 warps][CT] doubles
-  static constexpr int kBytes = kRed + 4 * CT * 8;
+  static constexpr int kR = kBlo + kBBytes;            // 2 buffers
+  static constexpr int kCtl = kR + 2 * kRBuf;          // 16 barriers + tmem slot + abort
+  // After the last MMA the R buffers are reused for the [4 quarters][CT]
+  // double log-likelihood reduction.
+  static constexpr int kRed = kR;
+  static constexpr int kBytes = kCtl + 256;
+  static_assert(4 * CT * 8 <= 2 * kRBuf, "reduction scratch must fit the R buffers");
   static constexpr int kMTiles = KB / 2;               // 128-feature tiles of G
+  static constexpr uint32_t kTmemCols = (2 * CT + kMTiles * CT) <= 256 ? 256 : 512;
+  static_assert(kBytes + 1024 <= 232448, "shared memory over the sm_103a limit");
+};
+
+struct Bars {
+  uint64_t x_full[2], x_empty[2], z_full[2], z_empty[2], r_full[2], r_empty[2], g_done, drain;
 };
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&v);
+}
+
+__device__ __forceinline__ void named_barrier(int id, int nthreads) {
+  asm volatile("bar.sync %0, %1;" ::"r"(id), "r"(nthreads) : "memory");
+}
+
+// Wait that also gives up when another role has already aborted.
+__device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity,
+                                              volatile int* abort_flag) {
+  if (tc::mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = tc::globaltimer_ns();
+  while (true) {
+    if (tc::mbar_try_wait(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (tc::globaltimer_ns() - t0 > kWaitLimitNs) return false;
+  }
 }
 
 template <int KB, int CT>
@@ -73,8 +114,8 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
                  int grid, double* __restrict__ lpart, float* __restrict__ gpart,
                  int* __restrict__ err) {
   using L = TcLayout<KB, CT>;
+  constexpr int kHalf = CT / 2;                 // chains per epilogue warp
   extern __shared__ __align__(1024) unsigned char smem_raw[];
-  // Dynamic shared memory is only guaranteed 16-byte aligned: round up.
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
   const int n = *n_dev;
@@ -86,27 +127,34 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
   const int c0 = tile * CT;
   const int rt_begin = (int)((long long)split * row_tiles / S);
   const int rt_end = (int)((long long)(split + 1) * row_tiles / S);
+  const int T = rt_end - rt_begin;
 
   unsigned char* Xs = smem + L::kX;
   unsigned char* Bhi = smem + L::kBhi;
   unsigned char* Blo = smem + L::kBlo;
-  unsigned char* Rhi = smem + L::kRhi;
-  unsigned char* Rlo = smem + L::kRlo;
-  uint64_t* bar_x = reinterpret_cast<uint64_t*>(smem + L::kCtl);
-  uint64_t* bar_z = bar_x + 1;
-  uint64_t* bar_g = bar_x + 2;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bar_x + 3);
+  unsigned char* Rs = smem + L::kR;
+  Bars* bars = reinterpret_cast<Bars*>(smem + L::kCtl);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::kCtl + sizeof(Bars));
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
   double* red = reinterpret_cast<double*>(smem + L::kRed);
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
-    tc::mbar_init(bar_x, 1);
-    tc::mbar_init(bar_z, 1);
-    tc::mbar_init(bar_g, 1);
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&bars->x_full[i], 1);
+      tc::mbar_init(&bars->x_empty[i], 1);
+      tc::mbar_init(&bars->z_full[i], 1);
+      tc::mbar_init(&bars->z_empty[i], kEpiWarps);
+      tc::mbar_init(&bars->r_full[i], kEpiWarps);
+      tc::mbar_init(&bars->r_empty[i], 1);
+    }
+    tc::mbar_init(&bars->g_done, 1);
+    tc::mbar_init(&bars->drain, 1);
+    *abort_flag = 0;
     tc::fence_mbar_init();
     tc::prefetch_tmap(&xmap);
   }
-  if (warp == 0) tc::tmem_alloc(tmem_slot, kTmemCols);
+  if (warp == 1) tc::tmem_alloc(tmem_slot, L::kTmemCols);
 
   // Chain states -> BF16 hi/lo, K-major 128-byte-swizzled [KB][CT][128 B].
   for (int i = tid; i < CT * KB * 8; i += kThreadsTc) {
@@ -126,8 +174,7 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
       const float2 hf = __bfloat1622float2(h);
       lo[e] = pack_bf16x2(v[2 * e] - hf.x, v[2 * e + 1] - hf.y);
     }
-    const int kb = d0 >> 6;
-    const uint32_t off = kb * (CT * 128) + tc::sw128_offset(c, d0 & 63);
+    const uint32_t off = (d0 >> 6) * (CT * 128) + tc::sw128_offset(c, d0 & 63);
     *reinterpret_cast<uint4*>(Bhi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
     *reinterpret_cast<uint4*>(Blo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
   }
@@ -136,172 +183,205 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
   __syncthreads();
   tc::tc_fence_after();
   const uint32_t tmem = *tmem_slot;
-  const uint32_t tz = tmem;               // Z: columns [0, CT)
-  const uint32_t tg = tmem + CT;          // G: columns [CT, CT * (1 + KB/2))
-  const uint32_t lane_base = (uint32_t)(warp * 32) << 16;
 
-  constexpr uint32_t idesc1 = tc::idesc_bf16_f32(128, CT, false, false);  // K-major A, B
-  constexpr uint32_t idesc2 = tc::idesc_bf16_f32(128, CT, true, true);    // MN-major A, B
-  const uint32_t xs_a = tc::smem_u32(Xs), bhi_a = tc::smem_u32(Bhi), blo_a = tc::smem_u32(Blo);
-  const uint32_t rhi_a = tc::smem_u32(Rhi), rlo_a = tc::smem_u32(Rlo);
-
-  float lp_acc[CT];
-#pragma unroll
-  for (int c = 0; c < CT; ++c) lp_acc[c] = 0.f;
-
-  bool ok = true;
-  int it = 0;
-  for (int rt = rt_begin; rt < rt_end && ok; ++rt, ++it) {
-    const uint32_t ph = it & 1;
-    if (tid == 0) {
-      tc::mbar_arrive_expect_tx(bar_x, L::kXBytes);
-#pragma unroll
-      for (int kb = 0; kb < KB; ++kb)
-        tc::tma_load_2d(Xs + kb * 16384, &xmap, kb * 64, rt * kRows, bar_x);
-    }
-    ok = tc::mbar_wait(bar_x, ph, kWaitLimitNs);
-    if (!__syncthreads_and(ok)) {
-      if (tid == 0) atomicExch(err, kTcTimeoutTma);
-      ok = false;
-      break;
-    }
-    // GEMM1: Z = X B^T (B = hi + lo).
-    if (tid == 0) {
-      tc::tc_fence_after();
-#pragma unroll
-      for (int kb = 0; kb < KB; ++kb) {
-#pragma unroll
-        for (int k = 0; k < 4; ++k) {
-          const uint64_t a = tc::smem_desc_sw128(xs_a + kb * 16384 + k * 32, 16, 1024);
-          const uint64_t bh = tc::smem_desc_sw128(bhi_a + kb * (CT * 128) + k * 32, 16, 1024);
-          const uint64_t bl = tc::smem_desc_sw128(blo_a + kb * (CT * 128) + k * 32, 16, 1024);
-          tc::mma_bf16(tz, a, bh, idesc1, (kb | k) ? 1u : 0u);
-          tc::mma_bf16(tz, a, bl, idesc1, 1u);
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      int it = 0;
+      for (; it < T; ++it) {
+        const int s = it & 1;
+        const uint32_t use = (uint32_t)(it >> 1);
+        if (!wait_or_abort(&bars->x_empty[s], (use & 1) ^ 1, abort_flag)) {
+          atomicExch(err, kTcTimeoutTma);
+          *abort_flag = 1;
+          break;
         }
+        tc::mbar_arrive_expect_tx(&bars->x_full[s], L::kXStage);
+#pragma unroll
+        for (int kb = 0; kb < KB; ++kb)
+          tc::tma_load_2d(Xs + s * L::kXStage + kb * 16384, &xmap, kb * 64,
+                          (rt_begin + it) * kRows, &bars->x_full[s]);
       }
-      tc::mma_commit(bar_z);
+      // Drain: every issued load has landed before the CTA can exit.
+      for (int j = (it > 2 ? it - 2 : 0); j < it; ++j)
+        tc::mbar_wait(&bars->x_full[j & 1], (uint32_t)((j >> 1) & 1), kWaitLimitNs);
     }
-    ok = tc::mbar_wait(bar_z, ph, kWaitLimitNs);
-    if (!__syncthreads_and(ok)) {
-      if (tid == 0) atomicExch(err, kTcTimeoutMma1);
-      ok = false;
-      break;
-    }
-    tc::tc_fence_after();
-    // Epilogue: thread owns row r = 32 * warp + lane of the tile.
-    const int r = warp * 32 + lane;
-    const int row = rt * kRows + r;
-    const bool valid = row < N;
-    const float yv = valid ? y[row] : 0.f;
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t idesc1 = tc::idesc_bf16_f32(128, CT, false, false);  // K-major A, B
+      constexpr uint32_t idesc2 = tc::idesc_bf16_f32(128, CT, true, true);    // MN-major A, B
+      const uint32_t xs_a = tc::smem_u32(Xs), bhi_a = tc::smem_u32(Bhi);
+      const uint32_t blo_a = tc::smem_u32(Blo), rs_a = tc::smem_u32(Rs);
+      const uint32_t tg = tmem + 2 * CT;
+      bool ok = true;
+      auto gemm1 = [&](int it) -> bool {
+        const int s = it & 1, b = it & 1;
+        const uint32_t use = (uint32_t)(it >> 1);
+        if (!wait_or_abort(&bars->x_full[s], use & 1, abort_flag)) return false;
+        if (!wait_or_abort(&bars->z_empty[b], (use & 1) ^ 1, abort_flag)) return false;
+        tc::tc_fence_after();
+        const uint32_t tz = tmem + b * CT;
+        const uint32_t xa = xs_a + s * L::kXStage;
 #pragma unroll
-    for (int ch = 0; ch < CT / 16; ++ch) {
-      float z[16];
-      tc::tmem_ld16(tz + lane_base + ch * 16, z);
-      tc::tmem_ld_wait();
-      float rv[16];
+        for (int kb = 0; kb < KB; ++kb) {
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const float zz = z[j];
-        // bernoulli.py:126-140: -softplus(z)(1-y) - softplus(-z) y
-        const float t = __expf(-fabsf(zz));
-        const float l1p = log1pf(t);
-        const float sp_pos = fmaxf(zz, 0.f) + l1p;   // softplus(z)
-        const float sp_neg = sp_pos - zz;            // softplus(-z)
-        const float lp = -sp_pos * (1.f - yv) - sp_neg * yv;
-        const float inv = __frcp_rn(1.f + t);
-        const float sig = zz >= 0.f ? inv : t * inv;
-        lp_acc[ch * 16 + j] += valid ? lp : 0.f;
-        rv[j] = valid ? (yv - sig) : 0.f;
-      }
-      // R tile, MN-major (chains contiguous), [CT/64][128 rows][128 B].
-#pragma unroll
-      for (int half = 0; half < 2; ++half) {
-        const int c = ch * 16 + half * 8;
-        uint32_t hi[4], lo[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float a = rv[half * 8 + 2 * e], b = rv[half * 8 + 2 * e + 1];
-          const __nv_bfloat162 h = __floats2bfloat162_rn(a, b);
-          hi[e] = *reinterpret_cast<const uint32_t*>(&h);
-          const float2 hf = __bfloat1622float2(h);
-          lo[e] = pack_bf16x2(a - hf.x, b - hf.y);
+          for (int k = 0; k < 4; ++k) {
+            const uint64_t a = tc::smem_desc_sw128(xa + kb * 16384 + k * 32, 16, 1024);
+            const uint64_t bh = tc::smem_desc_sw128(bhi_a + kb * (CT * 128) + k * 32, 16, 1024);
+            const uint64_t bl = tc::smem_desc_sw128(blo_a + kb * (CT * 128) + k * 32, 16, 1024);
+            tc::mma_bf16(tz, a, bh, idesc1, (kb | k) ? 1u : 0u);
+            tc::mma_bf16(tz, a, bl, idesc1, 1u);
+          }
         }
-        const uint32_t off = (c >> 6) * 16384 + tc::sw128_offset(r, c & 63);
-        *reinterpret_cast<uint4*>(Rhi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
-        *reinterpret_cast<uint4*>(Rlo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+        tc::mma_commit(&bars->z_full[b]);
+        return true;
+      };
+      if (T > 0) ok = gemm1(0);
+      for (int it = 0; it < T && ok; ++it) {
+        if (it + 1 < T) {
+          ok = gemm1(it + 1);
+          if (!ok) break;
+        }
+        const int s = it & 1, b = it & 1;
+        const uint32_t use = (uint32_t)(it >> 1);
+        if (!wait_or_abort(&bars->r_full[b], use & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        tc::tc_fence_after();
+        const uint32_t xa = xs_a + s * L::kXStage;
+        const uint32_t ra = rs_a + b * L::kRBuf;
+#pragma unroll
+        for (int mt = 0; mt < L::kMTiles; ++mt) {
+#pragma unroll
+          for (int ks = 0; ks < kRows / 16; ++ks) {
+            const uint64_t a = tc::smem_desc_sw128(xa + mt * 32768 + ks * 2048, 16384, 1024);
+            const uint64_t bd = tc::smem_desc_sw128(ra + ks * 2048, 16384, 1024);
+            tc::mma_bf16(tg + mt * CT, a, bd, idesc2, (it > 0 || ks > 0) ? 1u : 0u);
+          }
+        }
+        tc::mma_commit(&bars->x_empty[s]);
+        tc::mma_commit(&bars->r_empty[b]);
+      }
+      if (ok) {
+        tc::mma_commit(&bars->g_done);
+      } else {
+        atomicExch(err, kTcTimeoutMma);
+        *abort_flag = 1;
+      }
+      // Drain: all MMAs issued by this thread have completed.
+      tc::mma_commit(&bars->drain);
+      tc::mbar_wait(&bars->drain, 0, kWaitLimitNs);
+    }
+  } else {
+    // ---------------- epilogue (8 warps) ----------------
+    const int quarter = warp & 3;                 // TMEM lanes 32*quarter ..
+    const int half = (warp - 2) >> 2;             // chains [half*kHalf, +kHalf)
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    const int r = quarter * 32 + lane;            // row of the tile this thread owns
+    float lp_acc[kHalf];
+#pragma unroll
+    for (int c = 0; c < kHalf; ++c) lp_acc[c] = 0.f;
+    bool ok = true;
+    for (int it = 0; it < T; ++it) {
+      const int b = it & 1;
+      const uint32_t use = (uint32_t)(it >> 1);
+      if (!wait_or_abort(&bars->z_full[b], use & 1, abort_flag) ||
+          !wait_or_abort(&bars->r_empty[b], (use & 1) ^ 1, abort_flag)) {
+        ok = false;
+        break;
+      }
+      tc::tc_fence_after();
+      const int row = (rt_begin + it) * kRows + r;
+      const bool valid = row < N;
+      const float yv = valid ? y[row] : 0.f;
+      const uint32_t tz = tmem + b * CT + half * kHalf;
+      unsigned char* Rb = Rs + b * L::kRBuf;
+#pragma unroll
+      for (int ch = 0; ch < kHalf / 16; ++ch) {
+        float z[16];
+        tc::tmem_ld16(tz + lane_base + ch * 16, z);
+        tc::tmem_ld_wait();
+        float rv[16];
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const float zz = z[j];
+          // softplus(z) = max(z, 0) + log1p(exp(-|z|)); sigmoid from the same t.
+          const float t = __expf(-fabsf(zz));
+          const float l1p = __logf(1.f + t);
+          const float sp = fmaxf(zz, 0.f) + l1p;
+          const float lp = fmaf(yv, zz, -sp);          // y z - softplus(z)
+          const float inv = __frcp_rn(1.f + t);
+          const float sig = zz >= 0.f ? inv : t * inv;
+          lp_acc[ch * 16 + j] += valid ? lp : 0.f;
+          rv[j] = valid ? (yv - sig) : 0.f;
+        }
+        const int c = half * kHalf + ch * 16;
+        const uint32_t off0 = (c >> 6) * 16384 + tc::sw128_offset(r, c & 63);
+        const uint32_t off1 = ((c + 8) >> 6) * 16384 + tc::sw128_offset(r, (c + 8) & 63);
+        *reinterpret_cast<uint4*>(Rb + off0) =
+            make_uint4(pack_bf16x2(rv[0], rv[1]), pack_bf16x2(rv[2], rv[3]),
+                       pack_bf16x2(rv[4], rv[5]), pack_bf16x2(rv[6], rv[7]));
+        *reinterpret_cast<uint4*>(Rb + off1) =
+            make_uint4(pack_bf16x2(rv[8], rv[9]), pack_bf16x2(rv[10], rv[11]),
+                       pack_bf16x2(rv[12], rv[13]), pack_bf16x2(rv[14], rv[15]));
+      }
+      tc::tc_fence_before();
+      tc::fence_proxy_async_smem();
+      __syncwarp();
+      if (lane == 0) {
+        tc::mbar_arrive(&bars->z_empty[b]);
+        tc::mbar_arrive(&bars->r_full[b]);
       }
     }
-    tc::fence_proxy_async_smem();
-    tc::tc_fence_before();
-    __syncthreads();
-    // GEMM2: G += X^T R (R = hi + lo), per 128-feature tile of G.
-    if (tid == 0) {
+    if (ok && T > 0) ok = wait_or_abort(&bars->g_done, 0, abort_flag);
+    if (!ok) {
+      atomicExch(err, kTcTimeoutEpilogue);
+      *abort_flag = 1;
+    } else {
       tc::tc_fence_after();
+      // Gradient partials: TMEM lane = feature, column = chain.
 #pragma unroll
       for (int mt = 0; mt < L::kMTiles; ++mt) {
+        const int d = mt * 128 + quarter * 32 + lane;
 #pragma unroll
-        for (int ks = 0; ks < kRows / 16; ++ks) {
-          const uint64_t a = tc::smem_desc_sw128(xs_a + mt * 2 * 16384 + ks * 2048, 16384, 1024);
-          const uint64_t bh = tc::smem_desc_sw128(rhi_a + ks * 2048, 16384, 1024);
-          const uint64_t bl = tc::smem_desc_sw128(rlo_a + ks * 2048, 16384, 1024);
-          tc::mma_bf16(tg + mt * CT, a, bh, idesc2, (it > 0 || ks > 0) ? 1u : 0u);
-          tc::mma_bf16(tg + mt * CT, a, bl, idesc2, 1u);
-        }
-      }
-      tc::mma_commit(bar_g);
-    }
-    ok = tc::mbar_wait(bar_g, ph, kWaitLimitNs);
-    if (!__syncthreads_and(ok)) {
-      if (tid == 0) atomicExch(err, kTcTimeoutMma2);
-      ok = false;
-      break;
-    }
-  }
-
-  if (ok) {
-    tc::tc_fence_after();
-    // Gradient partials: TMEM lane = feature, column = chain.
-    if (it > 0) {
-#pragma unroll
-      for (int mt = 0; mt < L::kMTiles; ++mt) {
-        const int d = mt * 128 + warp * 32 + lane;
-#pragma unroll
-        for (int ch = 0; ch < CT / 16; ++ch) {
+        for (int ch = 0; ch < kHalf / 16; ++ch) {
           float g[16];
-          tc::tmem_ld16(tg + mt * CT + lane_base + ch * 16, g);
+          tc::tmem_ld16(tmem + 2 * CT + mt * CT + half * kHalf + lane_base + ch * 16, g);
           tc::tmem_ld_wait();
           if (d < D) {
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-              const int c = c0 + ch * 16 + j;
+              const int c = c0 + half * kHalf + ch * 16 + j;
               if (c < n) gpart[((size_t)split * n + c) * D + d] = g[j];
             }
           }
         }
       }
-    } else {
-      for (int i = tid; i < CT * D; i += kThreadsTc) {
-        const int c = c0 + i / D;
-        if (c < n) gpart[((size_t)split * n + c) * D + i % D] = 0.f;
+      // Log-likelihood partials: sum over the 128 rows per chain.
+#pragma unroll
+      for (int c = 0; c < kHalf; ++c) {
+        double v = (double)lp_acc[c];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) red[quarter * CT + half * kHalf + c] = v;
       }
     }
-    // Log-likelihood partials: sum over the 128 rows (threads) per chain.
-#pragma unroll
-    for (int c = 0; c < CT; ++c) {
-      double v = (double)lp_acc[c];
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-      if (lane == 0) red[warp * CT + c] = v;
-    }
-    __syncthreads();
-    for (int c = tid; c < CT; c += kThreadsTc) {
-      const double s = red[c] + red[CT + c] + red[2 * CT + c] + red[3 * CT + c];
-      if (c0 + c < n) lpart[(size_t)split * n + c0 + c] = s;
+    named_barrier(1, 32 * kEpiWarps);
+    if (ok) {
+      for (int c = tid - 64; c < CT; c += 32 * kEpiWarps) {
+        const double sum = red[c] + red[CT + c] + red[2 * CT + c] + red[3 * CT + c];
+        if (c0 + c < n) lpart[(size_t)split * n + c0 + c] = sum;
+      }
     }
   }
   tc::tc_fence_before();
   __syncthreads();
-  if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, L::kTmemCols);
+  }
 }
 
 __global__ void tc_reduce_kernel(const double* __restrict__ lpart, const float* __restrict__ gpart,
@@ -314,19 +394,20 @@ __global__ void tc_reduce_kernel(const double* __restrict__ lpart, const float* 
   const int lane = threadIdx.x & 31;
   if (warp >= n) return;
   const float* q = Q + (size_t)warp * ldq;
+  const size_t sstride = (size_t)n * D;
   double prior = 0.0;
   for (int d = lane; d < D; d += 32) {
     const float qd = q[d];
-    float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+    const float* p = gpart + (size_t)warp * D + d;
+    float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
     int s = 0;
-    for (; s + 4 <= S; s += 4) {
-      a0 += gpart[((size_t)(s + 0) * n + warp) * D + d];
-      a1 += gpart[((size_t)(s + 1) * n + warp) * D + d];
-      a2 += gpart[((size_t)(s + 2) * n + warp) * D + d];
-      a3 += gpart[((size_t)(s + 3) * n + warp) * D + d];
+    for (; s + 8 <= S; s += 8) {
+#pragma unroll
+      for (int u = 0; u < 8; ++u) a[u] += p[(size_t)(s + u) * sstride];
     }
-    for (; s < S; ++s) a0 += gpart[((size_t)s * n + warp) * D + d];
-    grad[(size_t)warp * ldg + d] = ((a0 + a1) + (a2 + a3)) - qd * inv_var;
+    for (; s < S; ++s) a[0] += p[(size_t)s * sstride];
+    const float tot = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
+    grad[(size_t)warp * ldg + d] = tot - qd * inv_var;
     prior += (double)qd * (double)qd;
   }
   prior = warp_sum(prior);
