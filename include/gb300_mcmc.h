@@ -88,7 +88,9 @@ GBM_API int gbm_target_dim(const gbm_target* target, int64_t* dim);
 
 /* Batched log-density and gradient at `chains` states (the value-and-gradient
  * call of mcmc/internal/util.py:246-283).  log_prob: float64 [chains];
- * grad: float32 [chains][dim]. */
+ * grad: float32 [chains][dim].  Asynchronous on the context stream; a
+ * bounded device wait that timed out in an earlier call is reported here
+ * (GBM_ETIMEDOUT) or by gbm_context_synchronize. */
 GBM_API int gbm_target_log_prob_and_grad(gbm_target* target, const float* state, int64_t chains,
                                  double* log_prob, float* grad);
 

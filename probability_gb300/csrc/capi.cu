@@ -95,6 +95,11 @@ int gbm_context_create(int device, void* stream, gbm_context** out) {
     GBM_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
     ctx->host_flag_slots = 16;
     GBM_CUDA(cudaMallocHost(&ctx->host_flags, sizeof(int) * ctx->host_flag_slots));
+    void* errp = nullptr;
+    GBM_CUDA(cudaHostAlloc(&errp, 64, cudaHostAllocMapped));
+    ctx->err_host = static_cast<volatile int*>(errp);
+    *ctx->err_host = 0;
+    GBM_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->err_dev), errp, 0));
     *out = ctx;
     return GBM_OK;
   });
@@ -106,6 +111,7 @@ int gbm_context_destroy(gbm_context* ctx) {
     DeviceGuard g(ctx->device);
     cudaStreamSynchronize(ctx->stream);
     if (ctx->host_flags) cudaFreeHost(ctx->host_flags);
+    if (ctx->err_host) cudaFreeHost(const_cast<int*>(ctx->err_host));
     if (ctx->owns_stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return GBM_OK;
@@ -117,6 +123,7 @@ int gbm_context_synchronize(gbm_context* ctx) {
   return guarded([&] {
     DeviceGuard g(ctx->device);
     GBM_CUDA(cudaStreamSynchronize(ctx->stream));
+    gbm::check_device_error(ctx);
     return GBM_OK;
   });
 }
@@ -196,16 +203,17 @@ int gbm_target_log_prob_and_grad(gbm_target* t, const float* state, int64_t chai
   return guarded([&] {
     DeviceGuard g(t->ctx->device);
     cudaStream_t s = t->ctx->stream;
-    t->ws.reserve(t->impl->workspace_bytes(chains));
+    gbm::check_device_error(t->ctx);
+    const size_t need = t->impl->workspace_bytes(chains);
+    if (need > t->ws.bytes) {
+      // The workspace is about to be replaced: let earlier calls finish.
+      GBM_CUDA(cudaStreamSynchronize(s));
+      t->ws.reserve(need);
+    }
     const int n = (int)chains;
-    GBM_CUDA(cudaMemcpyAsync(t->count.ptr, &n, sizeof(int), cudaMemcpyHostToDevice, s));
+    gbm::set_count(t->count.as<int>(), n, s);
     t->impl->eval(state, (int)t->impl->dim, t->count.as<int>(), n, log_prob, grad,
                   (int)t->impl->dim, t->ws.ptr, s);
-    // The count word is host memory of this frame; finish the copy before
-    // returning.
-    GBM_CUDA(cudaStreamSynchronize(s));
-    const int e = t->impl->device_error(s);
-    if (e) throw gbm::DeviceTimeout{e};
     return GBM_OK;
   });
 }
@@ -256,6 +264,7 @@ int gbm_hmc_one_step(gbm_hmc* k, int64_t chains, const float* state,
   if (num_leapfrog_steps < 1) return invalid("gbm_hmc_one_step: num_leapfrog_steps must be >= 1");
   return guarded([&] {
     DeviceGuard g(k->target->ctx->device);
+    gbm::check_device_error(k->target->ctx);
     gbm::HmcOutputs out{next_state, next_tlp, next_grads, proposed_state, proposed_tlp,
                         proposed_grads, initial_momentum, final_momentum,
                         log_acceptance_correction, log_accept_ratio, is_accepted};

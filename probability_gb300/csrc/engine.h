@@ -16,6 +16,12 @@ struct gbm_context {
   // Pinned host words the host polls for NUTS loop control.
   int* host_flags = nullptr;
   int host_flag_slots = 0;
+  // Error word in mapped pinned host memory: kernels whose bounded device
+  // waits run out store a nonzero code through err_dev; the host reads
+  // err_host without synchronizing (the store is visible once the kernel has
+  // finished).
+  volatile int* err_host = nullptr;
+  int* err_dev = nullptr;
 };
 
 namespace gbm {
@@ -56,10 +62,19 @@ struct Target {
   virtual double bytes(int64_t n) const = 0;
   // Kernels one eval() launches (for launch accounting).
   virtual int launches_per_eval() const = 0;
-  // Error word written by kernels whose bounded device waits ran out
-  // (0 = none).  Synchronizes `s`.
-  virtual int device_error(cudaStream_t s) { (void)s; return 0; }
 };
+
+// Raise (and clear) an error a kernel stored in the context's error word.
+inline void check_device_error(gbm_context* ctx) {
+  const int e = ctx->err_host ? *ctx->err_host : 0;
+  if (e) {
+    *ctx->err_host = 0;
+    throw DeviceTimeout{e};
+  }
+}
+
+// Write the batch-size word `*count = n` on stream `s` (no host memory).
+void set_count(int* count, int n, cudaStream_t s);
 
 std::unique_ptr<Target> make_logreg_simt(gbm_context* ctx, const float* X, int64_t n,
                                          int64_t d, const float* y, float prior_scale);

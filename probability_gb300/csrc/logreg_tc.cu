@@ -34,6 +34,7 @@
 
 #include <algorithm>
 #include <memory>
+#include <cstdlib>
 #include <string>
 
 #include "engine.h"
@@ -43,9 +44,11 @@ namespace gbm {
 namespace {
 
 constexpr int kRows = 128;                         // rows of X per tile
-constexpr int kEpiWarps = 8;
-constexpr int kThreadsTc = 32 * (2 + kEpiWarps);   // 320
+// Threads of a CTA with EPI epilogue warps (plus the TMA and MMA warps).
+__host__ __device__ constexpr int tc_threads(int epi) { return 32 * (2 + epi); }
 constexpr uint64_t kWaitLimitNs = 2000000000ull;   // 2 s bound on every device wait
+constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kLn2 = 0.6931471805599453f;
 
 enum TcError : int {
   kTcOk = 0,
@@ -107,14 +110,16 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity,
   }
 }
 
-template <int KB, int CT>
-__global__ void __launch_bounds__(kThreadsTc, 1)
+template <int KB, int CT, int EPI>
+__global__ void __launch_bounds__(tc_threads(EPI), 1)
 logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restrict__ y, int N,
                  int D, const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev,
                  int grid, double* __restrict__ lpart, float* __restrict__ gpart,
                  int* __restrict__ err) {
   using L = TcLayout<KB, CT>;
-  constexpr int kHalf = CT / 2;                 // chains per epilogue warp
+  constexpr int kThreads = tc_threads(EPI);
+  constexpr int kCW = CT * 4 / EPI;             // chains per epilogue warp
+  static_assert(kCW == 32 || kCW == 64, "epilogue width");
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -144,8 +149,8 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
       tc::mbar_init(&bars->x_full[i], 1);
       tc::mbar_init(&bars->x_empty[i], 1);
       tc::mbar_init(&bars->z_full[i], 1);
-      tc::mbar_init(&bars->z_empty[i], kEpiWarps);
-      tc::mbar_init(&bars->r_full[i], kEpiWarps);
+      tc::mbar_init(&bars->z_empty[i], EPI);
+      tc::mbar_init(&bars->r_full[i], EPI);
       tc::mbar_init(&bars->r_empty[i], 1);
     }
     tc::mbar_init(&bars->g_done, 1);
@@ -157,7 +162,7 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
   if (warp == 1) tc::tmem_alloc(tmem_slot, L::kTmemCols);
 
   // Chain states -> BF16 hi/lo, K-major 128-byte-swizzled [KB][CT][128 B].
-  for (int i = tid; i < CT * KB * 8; i += kThreadsTc) {
+  for (int i = tid; i < CT * KB * 8; i += kThreads) {
     const int c = i / (KB * 8), chunk = i % (KB * 8);
     const int d0 = chunk * 8;
     float v[8];
@@ -192,7 +197,7 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
         const int s = it & 1;
         const uint32_t use = (uint32_t)(it >> 1);
         if (!wait_or_abort(&bars->x_empty[s], (use & 1) ^ 1, abort_flag)) {
-          atomicExch(err, kTcTimeoutTma);
+          tc::record_error(err,kTcTimeoutTma);
           *abort_flag = 1;
           break;
         }
@@ -267,7 +272,7 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
       if (ok) {
         tc::mma_commit(&bars->g_done);
       } else {
-        atomicExch(err, kTcTimeoutMma);
+        tc::record_error(err,kTcTimeoutMma);
         *abort_flag = 1;
       }
       // Drain: all MMAs issued by this thread have completed.
@@ -275,15 +280,21 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
       tc::mbar_wait(&bars->drain, 0, kWaitLimitNs);
     }
   } else {
-    // ---------------- epilogue (8 warps) ----------------
+    // ---------------- epilogue (EPI warps) ----------------
     const int quarter = warp & 3;                 // TMEM lanes 32*quarter ..
-    const int half = (warp - 2) >> 2;             // chains [half*kHalf, +kHalf)
+    const int half = (warp - 2) >> 2;             // chains [half*kCW, +kCW)
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const int r = quarter * 32 + lane;            // row of the tile this thread owns
-    float lp_acc[kHalf];
+    float lp_acc[kCW];
 #pragma unroll
-    for (int c = 0; c < kHalf; ++c) lp_acc[c] = 0.f;
+    for (int c = 0; c < kCW; ++c) lp_acc[c] = 0.f;
     bool ok = true;
+    // y of this thread's row, prefetched one tile ahead.
+    float y_next = 0.f;
+    {
+      const int row0 = rt_begin * kRows + r;
+      if (T > 0 && row0 < N) y_next = y[row0];
+    }
     for (int it = 0; it < T; ++it) {
       const int b = it & 1;
       const uint32_t use = (uint32_t)(it >> 1);
@@ -295,29 +306,37 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
       tc::tc_fence_after();
       const int row = (rt_begin + it) * kRows + r;
       const bool valid = row < N;
-      const float yv = valid ? y[row] : 0.f;
-      const uint32_t tz = tmem + b * CT + half * kHalf;
+      const float yv = valid ? y_next : 0.f;
+      if (it + 1 < T && row + kRows < N) y_next = y[row + kRows];
+      const uint32_t tz = tmem + b * CT + half * kCW;
       unsigned char* Rb = Rs + b * L::kRBuf;
+      float zall[kCW];
 #pragma unroll
-      for (int ch = 0; ch < kHalf / 16; ++ch) {
-        float z[16];
-        tc::tmem_ld16(tz + lane_base + ch * 16, z);
-        tc::tmem_ld_wait();
+      for (int q = 0; q < kCW / 32; ++q) tc::tmem_ld32(tz + lane_base + q * 32, zall + q * 32);
+      tc::tmem_ld_wait();
+#pragma unroll
+      for (int ch = 0; ch < kCW / 16; ++ch) {
+        const float* z = zall + ch * 16;
         float rv[16];
+        // log Bernoulli(y | z) = y z - softplus(z), softplus(z) = max(z, 0) +
+        // ln2 * log2(1 + 2^(-|z| log2 e)).  The sigmoid only feeds the BF16
+        // gradient contraction, so the tanh form 0.5 + 0.5 tanh(z / 2) (one
+        // special-function op) is accurate enough for it.
+        if (valid) {
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-          const float zz = z[j];
-          // softplus(z) = max(z, 0) + log1p(exp(-|z|)); sigmoid from the same t.
-          const float t = __expf(-fabsf(zz));
-          const float l1p = __logf(1.f + t);
-          const float sp = fmaxf(zz, 0.f) + l1p;
-          const float lp = fmaf(yv, zz, -sp);          // y z - softplus(z)
-          const float inv = __frcp_rn(1.f + t);
-          const float sig = zz >= 0.f ? inv : t * inv;
-          lp_acc[ch * 16 + j] += valid ? lp : 0.f;
-          rv[j] = valid ? (yv - sig) : 0.f;
+          for (int j = 0; j < 16; ++j) {
+            const float zz = z[j];
+            const float t = tc::ex2_approx(-fabsf(zz) * kLog2e);
+            const float lg = tc::lg2_approx(1.f + t);
+            lp_acc[ch * 16 + j] =
+                fmaf(-kLn2, lg, lp_acc[ch * 16 + j] + fmaf(yv, zz, -fmaxf(zz, 0.f)));
+            rv[j] = yv - fmaf(0.5f, tc::tanh_approx(0.5f * zz), 0.5f);
+          }
+        } else {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) rv[j] = 0.f;   // rows past N
         }
-        const int c = half * kHalf + ch * 16;
+        const int c = half * kCW + ch * 16;
         const uint32_t off0 = (c >> 6) * 16384 + tc::sw128_offset(r, c & 63);
         const uint32_t off1 = ((c + 8) >> 6) * 16384 + tc::sw128_offset(r, (c + 8) & 63);
         *reinterpret_cast<uint4*>(Rb + off0) =
@@ -337,7 +356,7 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
     }
     if (ok && T > 0) ok = wait_or_abort(&bars->g_done, 0, abort_flag);
     if (!ok) {
-      atomicExch(err, kTcTimeoutEpilogue);
+      tc::record_error(err,kTcTimeoutEpilogue);
       *abort_flag = 1;
     } else {
       tc::tc_fence_after();
@@ -346,14 +365,14 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
       for (int mt = 0; mt < L::kMTiles; ++mt) {
         const int d = mt * 128 + quarter * 32 + lane;
 #pragma unroll
-        for (int ch = 0; ch < kHalf / 16; ++ch) {
+        for (int ch = 0; ch < kCW / 16; ++ch) {
           float g[16];
-          tc::tmem_ld16(tmem + 2 * CT + mt * CT + half * kHalf + lane_base + ch * 16, g);
+          tc::tmem_ld16(tmem + 2 * CT + mt * CT + half * kCW + lane_base + ch * 16, g);
           tc::tmem_ld_wait();
           if (d < D) {
 #pragma unroll
             for (int j = 0; j < 16; ++j) {
-              const int c = c0 + half * kHalf + ch * 16 + j;
+              const int c = c0 + half * kCW + ch * 16 + j;
               if (c < n) gpart[((size_t)split * n + c) * D + d] = g[j];
             }
           }
@@ -361,16 +380,18 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
       }
       // Log-likelihood partials: sum over the 128 rows per chain.
 #pragma unroll
-      for (int c = 0; c < kHalf; ++c) {
-        double v = (double)lp_acc[c];
+      // (FP32 shuffles: the FP64 pipe of this GPU is far too narrow for a
+      // per-chain warp reduction; only the final 4-way sum is FP64.)
+      for (int c = 0; c < kCW; ++c) {
+        float v = lp_acc[c];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        if (lane == 0) red[quarter * CT + half * kHalf + c] = v;
+        if (lane == 0) red[quarter * CT + half * kCW + c] = (double)v;
       }
     }
-    named_barrier(1, 32 * kEpiWarps);
+    named_barrier(1, 32 * EPI);
     if (ok) {
-      for (int c = tid - 64; c < CT; c += 32 * kEpiWarps) {
+      for (int c = tid - 64; c < CT; c += 32 * EPI) {
         const double sum = red[c] + red[CT + c] + red[2 * CT + c] + red[3 * CT + c];
         if (c0 + c < n) lpart[(size_t)split * n + c0 + c] = sum;
       }
@@ -393,29 +414,34 @@ __global__ void tc_reduce_kernel(const double* __restrict__ lpart, const float* 
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   if (warp >= n) return;
+  // Each lane owns features lane + 32k (k < 8, D <= 256): all of them are
+  // loaded for one split before the next, so a warp keeps up to 256
+  // independent loads in flight; splits are summed in fixed order.
   const float* q = Q + (size_t)warp * ldq;
   const size_t sstride = (size_t)n * D;
-  double prior = 0.0;
-  for (int d = lane; d < D; d += 32) {
-    const float qd = q[d];
-    const float* p = gpart + (size_t)warp * D + d;
-    float a[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-    int s = 0;
-    for (; s + 8 <= S; s += 8) {
+  const float* p = gpart + (size_t)warp * D;
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  double lp = 0.0;
+  for (int s = 0; s < S; ++s) {
 #pragma unroll
-      for (int u = 0; u < 8; ++u) a[u] += p[(size_t)(s + u) * sstride];
+    for (int k = 0; k < 8; ++k) {
+      const int d = lane + 32 * k;
+      if (d < D) acc[k] += p[(size_t)s * sstride + d];
     }
-    for (; s < S; ++s) a[0] += p[(size_t)s * sstride];
-    const float tot = ((a[0] + a[1]) + (a[2] + a[3])) + ((a[4] + a[5]) + (a[6] + a[7]));
-    grad[(size_t)warp * ldg + d] = tot - qd * inv_var;
-    prior += (double)qd * (double)qd;
+    if (lane == 0) lp += lpart[(size_t)s * n + warp];
+  }
+  double prior = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const int d = lane + 32 * k;
+    if (d < D) {
+      const float qd = q[d];
+      grad[(size_t)warp * ldg + d] = acc[k] - qd * inv_var;
+      prior += (double)qd * (double)qd;
+    }
   }
   prior = warp_sum(prior);
-  if (lane == 0) {
-    double lp = 0.0;
-    for (int s = 0; s < S; ++s) lp += lpart[(size_t)s * n + warp];
-    logp[warp] = lp - 0.5 * (double)inv_var * prior + (double)D * log_norm;
-  }
+  if (lane == 0) logp[warp] = lp - 0.5 * (double)inv_var * prior + (double)D * log_norm;
 }
 
 __global__ void to_bf16_padded(const float* __restrict__ X, int64_t N, int D, int Dp,
@@ -466,7 +492,7 @@ class LogregTc final : public Target {
     const int Dp = kb_ * 64;
     xb_.reserve(sizeof(__nv_bfloat16) * (size_t)N_ * Dp);
     y_.reserve(sizeof(float) * (size_t)N_);
-    err_.reserve(256);
+    err_dev_ = ctx->err_dev;
     const int64_t total = N_ * Dp;
     const int tb = 256;
     const int64_t blocks = (total + tb - 1) / tb;
@@ -479,7 +505,6 @@ class LogregTc final : public Target {
     GBM_CUDA(cudaGetLastError());
     GBM_CUDA(cudaMemcpyAsync(y_.ptr, y, sizeof(float) * N_, cudaMemcpyDeviceToDevice,
                              ctx->stream));
-    GBM_CUDA(cudaMemsetAsync(err_.ptr, 0, 256, ctx->stream));
     inv_var_ = 1.f / (prior_scale * prior_scale);
     log_norm_ = -log((double)prior_scale) - 0.5 * log(2.0 * M_PI);
     grid_ = ctx->num_sms;
@@ -495,12 +520,17 @@ class LogregTc final : public Target {
                                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) throw CudaError{cudaErrorInvalidValue, "cuTensorMapEncodeTiled"};
     smem_ = (kb_ == 2 ? TcLayout<2, 128>::kBytes : TcLayout<4, 64>::kBytes) + 1024;
-    if (kb_ == 2)
-      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<2, 128>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_));
-    else
-      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<4, 64>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_));
+    // Epilogue width: 16 warps by default; GBM_TC_EPI=8 selects 8 (tuning).
+    const char* e = getenv("GBM_TC_EPI");
+    epi_ = (e && atoi(e) == 8) ? 8 : 16;
+    const int attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
+    if (kb_ == 2) {
+      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<2, 128, 8>, (cudaFuncAttribute)attr, (int)smem_));
+      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<2, 128, 16>, (cudaFuncAttribute)attr, (int)smem_));
+    } else {
+      epi_ = 8;  // 64-chain tiles: 32 chains per epilogue warp
+      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<4, 64, 8>, (cudaFuncAttribute)attr, (int)smem_));
+    }
   }
 
   size_t workspace_bytes(int64_t cap) const override {
@@ -514,23 +544,19 @@ class LogregTc final : public Target {
     double* lpart = static_cast<double*>(ws);
     float* gpart = reinterpret_cast<float*>(lpart + rows);
     const int N = (int)N_, D = (int)D_;
-    if (kb_ == 2)
-      logreg_tc_kernel<2, 128><<<grid_, kThreadsTc, smem_, s>>>(
-          xmap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_.as<int>());
-    else
-      logreg_tc_kernel<4, 64><<<grid_, kThreadsTc, smem_, s>>>(
-          xmap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_.as<int>());
+#define GBM_TC_LAUNCH(KB_, CT_, EPI_)                                                     \
+  logreg_tc_kernel<KB_, CT_, EPI_><<<grid_, tc_threads(EPI_), smem_, s>>>(                \
+      xmap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_dev_)
+    if (kb_ == 2) {
+      if (epi_ == 8) GBM_TC_LAUNCH(2, 128, 8); else GBM_TC_LAUNCH(2, 128, 16);
+    } else {
+      GBM_TC_LAUNCH(4, 64, 8);
+    }
+#undef GBM_TC_LAUNCH
     GBM_CUDA(cudaGetLastError());
     tc_reduce_kernel<<<(cap + 7) / 8, 256, 0, s>>>(lpart, gpart, q, ldq, n_dev, ct_, grid_, N, D,
                                                    inv_var_, log_norm_, logp, grad, ldg);
     GBM_CUDA(cudaGetLastError());
-  }
-
-  int device_error(cudaStream_t s) override {
-    int e = 0;
-    GBM_CUDA(cudaMemcpyAsync(&e, err_.ptr, sizeof(int), cudaMemcpyDeviceToHost, s));
-    GBM_CUDA(cudaStreamSynchronize(s));
-    return e;
   }
 
   int launches_per_eval() const override { return 2; }
@@ -541,11 +567,12 @@ class LogregTc final : public Target {
 
  private:
   int64_t N_, D_;
-  int kb_ = 2, ct_ = 128, grid_ = 0;
+  int kb_ = 2, ct_ = 128, grid_ = 0, epi_ = 16;
   size_t smem_ = 0;
   float inv_var_ = 1.f;
   double log_norm_ = 0.0;
-  DeviceBuffer xb_, y_, err_;
+  DeviceBuffer xb_, y_;
+  int* err_dev_ = nullptr;
   CUtensorMap xmap_;
 };
 

@@ -77,6 +77,13 @@ __global__ void build_active_kernel(const uint8_t* __restrict__ flags, uint8_t b
   if (tid == 0) *count = base_s;
 }
 
+__global__ void set_count_kernel(int* count, int n) { *count = n; }
+
+void set_count(int* count, int n, cudaStream_t s) {
+  set_count_kernel<<<1, 1, 0, s>>>(count, n);
+  GBM_CUDA(cudaGetLastError());
+}
+
 static void build_active(const NutsDev& d, uint8_t bit, cudaStream_t s) {
   build_active_kernel<<<1, 1024, 0, s>>>(d.flags, bit, d.C, d.act_idx, d.act_count);
   GBM_CUDA(cudaGetLastError());
@@ -607,8 +614,7 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
       GBM_CUDA(cudaMemcpyAsync(host_flags, w.any_cont, sizeof(int), cudaMemcpyDeviceToHost, s));
       GBM_CUDA(cudaStreamSynchronize(s));
       if (k->profiling) nuts_profile_flush(k);
-      const int dev_err = k->target->impl->device_error(s);
-      if (dev_err) throw DeviceTimeout{dev_err};
+      check_device_error(ctx);
       if (host_flags[0] == 0) break;
     }
     nuts_depth_begin_kernel<<<(int)((chains + tb - 1) / tb), tb, 0, s>>>(w, key, depth);
