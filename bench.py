@@ -35,7 +35,7 @@ sys.path.insert(0, ROOT)
 WORKLOADS = {
     'nuts_logreg_1e5x100': dict(n=100000, d=100, chains=1024, depth=10, seed=1,
                                 feature_scale=0.1, step0=0.1, target_accept=0.8,
-                                num_adaptation_steps=1000, precision='fp32'),
+                                num_adaptation_steps=1000, precision='mixed'),
 }
 METRIC = 'grad-evals/s (NUTS leapfrogs_taken summed over chains; min-ESS/s reported beside)'
 
@@ -362,6 +362,32 @@ def run_engine(args, w):
   h2d = C * D * 4 * 2 + C * 8
   d2h = C * D * 4 * 2 + C * 8 * 2
 
+  # ---- the plain FP32 form on the same GPU, from the same adapted state ----
+  plain = None
+  if target.precision != 'fp32' and args.plain_steps > 0:
+    t32 = pg.LogisticRegression(X, y, precision='fp32')
+    eps = kr.new_step_size.reshape(-1)[0].item()
+    n32 = pg.mcmc.NoUTurnSampler(t32, step_size=eps, max_tree_depth=w['depth'])
+    s32 = state.clone()
+    k32 = n32.bootstrap_results(s32)
+    for i in range(2):
+      s32, k32 = n32.one_step(s32, k32, seed=pg._util.step_key(seed, 10**6 + i))
+    lf32 = torch.zeros((), dtype=torch.int64, device=dev)
+    barrier()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for i in range(args.plain_steps):
+      s32, k32 = n32.one_step(s32, k32, seed=pg._util.step_key(seed, 2 * 10**6 + i))
+      lf32 += k32.leapfrogs_taken.sum()
+    e1.record()
+    e1.synchronize()
+    s = e0.elapsed_time(e1) / 1000.0
+    plain = {'value': int(lf32.item()) / s, 'unit': 'grad-evals/s',
+             'ms_per_step': 1000 * s / args.plain_steps, 'steps': args.plain_steps,
+             'note': 'NoUTurnSampler with the FP32 CUDA-core target at the adapted step size, '
+                     'started from the same chain state'}
+
   cpu = None
   if rank == 0 and world == 1 and not args.no_cpu_baseline:
     budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '20'))
@@ -397,6 +423,8 @@ def run_engine(args, w):
                 'd2h_bytes_per_step': d2h, 'steps': e2e_steps},
         'roofline': roofline,
         'cpu_baseline': cpu,
+        'plain_fp32': plain,
+        'speedup_vs_plain_fp32': (value / plain['value']) if plain else None,
         'gpu_launches': int(launches.value) + args.steps,
         'clocks': clk,
     }
@@ -416,6 +444,8 @@ def main():
   ap.add_argument('--workload', default='nuts_logreg_1e5x100', choices=sorted(WORKLOADS))
   ap.add_argument('--precision', default=None, choices=[None, 'fp32', 'mixed'])
   ap.add_argument('--no-cpu-baseline', action='store_true')
+  ap.add_argument('--plain-steps', type=int, default=10,
+                  help='transitions of the plain FP32 form timed beside the mixed path')
   ap.add_argument('--kernel-only', action='store_true',
                   help='time the batched log-prob+gradient alone (profiling aid)')
   args = ap.parse_args()

@@ -65,7 +65,7 @@ __host__ __device__ inline int tc_splits(int n, int ct, int grid, int row_tiles)
   return s > row_tiles ? row_tiles : s;
 }
 
-template <int KB, int CT>
+template <int KB, int CT, bool XLO>
 struct TcLayout {
   static constexpr int kXStage = KB * 16384;           // [KB][128 rows][128 B]
   static constexpr int kBBytes = KB * CT * 128;        // [KB][CT rows][128 B]
@@ -74,7 +74,8 @@ struct TcLayout {
   static constexpr int kBhi = kX + 2 * kXStage;
   static constexpr int kBlo = kBhi + kBBytes;
   static constexpr int kR = kBlo + kBBytes;            // 2 buffers
-  static constexpr int kCtl = kR + 2 * kRBuf;          // 16 barriers + tmem slot + abort
+  static constexpr int kXlo = kR + 2 * kRBuf;          // X residual, 1 stage (XLO only)
+  static constexpr int kCtl = kXlo + (XLO ? kXStage : 0);  // barriers + tmem slot + abort
   // After the last MMA the R buffers are reused for the [4 quarters][CT]
   // double log-likelihood reduction.
   static constexpr int kRed = kR;
@@ -87,6 +88,7 @@ struct TcLayout {
 
 struct Bars {
   uint64_t x_full[2], x_empty[2], z_full[2], z_empty[2], r_full[2], r_empty[2], g_done, drain;
+  uint64_t xlo_full, xlo_empty;
 };
 
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
@@ -110,13 +112,17 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity,
   }
 }
 
-template <int KB, int CT, int EPI>
+// XLO: X is FP32 data stored as X_hi + X_lo (both BF16); GEMM1 adds the
+// X_lo B_hi product so Z keeps ~16 significant bits of the FP32 data.  The
+// gradient contraction uses X_hi.
+template <int KB, int CT, int EPI, bool XLO>
 __global__ void __launch_bounds__(tc_threads(EPI), 1)
-logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restrict__ y, int N,
+logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
+                 const __grid_constant__ CUtensorMap xlomap, const float* __restrict__ y, int N,
                  int D, const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev,
                  int grid, double* __restrict__ lpart, float* __restrict__ gpart,
                  int* __restrict__ err) {
-  using L = TcLayout<KB, CT>;
+  using L = TcLayout<KB, CT, XLO>;
   constexpr int kThreads = tc_threads(EPI);
   constexpr int kCW = CT * 4 / EPI;             // chains per epilogue warp
   static_assert(kCW == 32 || kCW == 64, "epilogue width");
@@ -155,6 +161,8 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
     }
     tc::mbar_init(&bars->g_done, 1);
     tc::mbar_init(&bars->drain, 1);
+    tc::mbar_init(&bars->xlo_full, 1);
+    tc::mbar_init(&bars->xlo_empty, 1);
     *abort_flag = 0;
     tc::fence_mbar_init();
     tc::prefetch_tmap(&xmap);
@@ -206,10 +214,27 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
         for (int kb = 0; kb < KB; ++kb)
           tc::tma_load_2d(Xs + s * L::kXStage + kb * 16384, &xmap, kb * 64,
                           (rt_begin + it) * kRows, &bars->x_full[s]);
+        if constexpr (XLO) {
+          // Single X_lo buffer: free once GEMM1 of the previous tile is done.
+          if (!wait_or_abort(&bars->xlo_empty, (uint32_t)(it & 1) ^ 1, abort_flag)) {
+            tc::record_error(err, kTcTimeoutTma);
+            *abort_flag = 1;
+            ++it;
+            break;
+          }
+          tc::mbar_arrive_expect_tx(&bars->xlo_full, L::kXStage);
+#pragma unroll
+          for (int kb = 0; kb < KB; ++kb)
+            tc::tma_load_2d(smem + L::kXlo + kb * 16384, &xlomap, kb * 64,
+                            (rt_begin + it) * kRows, &bars->xlo_full);
+        }
       }
       // Drain: every issued load has landed before the CTA can exit.
       for (int j = (it > 2 ? it - 2 : 0); j < it; ++j)
         tc::mbar_wait(&bars->x_full[j & 1], (uint32_t)((j >> 1) & 1), kWaitLimitNs);
+      if constexpr (XLO) {
+        if (it > 0) tc::mbar_wait(&bars->xlo_full, (uint32_t)((it - 1) & 1), kWaitLimitNs);
+      }
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
@@ -225,9 +250,13 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
         const uint32_t use = (uint32_t)(it >> 1);
         if (!wait_or_abort(&bars->x_full[s], use & 1, abort_flag)) return false;
         if (!wait_or_abort(&bars->z_empty[b], (use & 1) ^ 1, abort_flag)) return false;
+        if constexpr (XLO) {
+          if (!wait_or_abort(&bars->xlo_full, (uint32_t)(it & 1), abort_flag)) return false;
+        }
         tc::tc_fence_after();
         const uint32_t tz = tmem + b * CT;
         const uint32_t xa = xs_a + s * L::kXStage;
+        const uint32_t xla = tc::smem_u32(smem + L::kXlo);
 #pragma unroll
         for (int kb = 0; kb < KB; ++kb) {
 #pragma unroll
@@ -237,9 +266,14 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restri
             const uint64_t bl = tc::smem_desc_sw128(blo_a + kb * (CT * 128) + k * 32, 16, 1024);
             tc::mma_bf16(tz, a, bh, idesc1, (kb | k) ? 1u : 0u);
             tc::mma_bf16(tz, a, bl, idesc1, 1u);
+            if constexpr (XLO) {
+              const uint64_t al = tc::smem_desc_sw128(xla + kb * 16384 + k * 32, 16, 1024);
+              tc::mma_bf16(tz, al, bh, idesc1, 1u);
+            }
           }
         }
         tc::mma_commit(&bars->z_full[b]);
+        if constexpr (XLO) tc::mma_commit(&bars->xlo_empty);
         return true;
       };
       if (T > 0) ok = gemm1(0);
@@ -444,13 +478,18 @@ __global__ void tc_reduce_kernel(const double* __restrict__ lpart, const float* 
   if (lane == 0) logp[warp] = lp - 0.5 * (double)inv_var * prior + (double)D * log_norm;
 }
 
+// FP32 X -> X_hi = bf16(X) and (optionally) X_lo = bf16(X - X_hi), zero-padded
+// to Dp features.
 __global__ void to_bf16_padded(const float* __restrict__ X, int64_t N, int D, int Dp,
-                               __nv_bfloat16* __restrict__ out) {
+                               __nv_bfloat16* __restrict__ out, __nv_bfloat16* __restrict__ lo) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N * Dp) return;
   const int64_t r = i / Dp;
   const int d = (int)(i % Dp);
-  out[i] = __float2bfloat16_rn(d < D ? X[r * D + d] : 0.f);
+  const float v = d < D ? X[r * D + d] : 0.f;
+  const __nv_bfloat16 h = __float2bfloat16_rn(v);
+  out[i] = h;
+  if (lo) lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
 __global__ void bf16_pad(const __nv_bfloat16* __restrict__ X, int64_t N, int D, int Dp,
@@ -489,8 +528,11 @@ class LogregTc final : public Target {
     dim = d;
     kb_ = d <= 128 ? 2 : 4;
     ct_ = kb_ == 2 ? 128 : 64;
+    // FP32 data up to 128 features keeps a BF16 residual X_lo (see XLO).
+    xlo_ = (x_dtype == 0 && kb_ == 2);
     const int Dp = kb_ * 64;
     xb_.reserve(sizeof(__nv_bfloat16) * (size_t)N_ * Dp);
+    if (xlo_) xl_.reserve(sizeof(__nv_bfloat16) * (size_t)N_ * Dp);
     y_.reserve(sizeof(float) * (size_t)N_);
     err_dev_ = ctx->err_dev;
     const int64_t total = N_ * Dp;
@@ -498,7 +540,8 @@ class LogregTc final : public Target {
     const int64_t blocks = (total + tb - 1) / tb;
     if (x_dtype == 0)
       to_bf16_padded<<<(unsigned)blocks, tb, 0, ctx->stream>>>(
-          static_cast<const float*>(X), N_, (int)D_, Dp, xb_.as<__nv_bfloat16>());
+          static_cast<const float*>(X), N_, (int)D_, Dp, xb_.as<__nv_bfloat16>(),
+          xlo_ ? xl_.as<__nv_bfloat16>() : nullptr);
     else
       bf16_pad<<<(unsigned)blocks, tb, 0, ctx->stream>>>(
           static_cast<const __nv_bfloat16*>(X), N_, (int)D_, Dp, xb_.as<__nv_bfloat16>());
@@ -508,28 +551,21 @@ class LogregTc final : public Target {
     inv_var_ = 1.f / (prior_scale * prior_scale);
     log_norm_ = -log((double)prior_scale) - 0.5 * log(2.0 * M_PI);
     grid_ = ctx->num_sms;
-    // Tensor map over X_bf16 [N][Dp]: boxes of 64 features x 128 rows,
-    // 128-byte swizzle, rows past N read as zeros.
-    cuuint64_t dims[2] = {(cuuint64_t)Dp, (cuuint64_t)N_};
-    cuuint64_t strides[1] = {(cuuint64_t)Dp * 2};
-    cuuint32_t box[2] = {64, (cuuint32_t)kRows};
-    cuuint32_t estr[2] = {1, 1};
-    CUresult r = encode_tiled()(&xmap_, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, xb_.ptr, dims,
-                                strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) throw CudaError{cudaErrorInvalidValue, "cuTensorMapEncodeTiled"};
-    smem_ = (kb_ == 2 ? TcLayout<2, 128>::kBytes : TcLayout<4, 64>::kBytes) + 1024;
-    // Epilogue width: 16 warps by default; GBM_TC_EPI=8 selects 8 (tuning).
-    const char* e = getenv("GBM_TC_EPI");
-    epi_ = (e && atoi(e) == 8) ? 8 : 16;
+    encode(&xmap_, xb_.ptr, Dp);
+    encode(&xlomap_, xlo_ ? xl_.ptr : xb_.ptr, Dp);
     const int attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
-    if (kb_ == 2) {
-      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<2, 128, 8>, (cudaFuncAttribute)attr, (int)smem_));
-      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<2, 128, 16>, (cudaFuncAttribute)attr, (int)smem_));
+    if (kb_ == 2 && xlo_) {
+      smem_ = TcLayout<2, 128, true>::kBytes + 1024;
+      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<2, 128, 16, true>, (cudaFuncAttribute)attr,
+                                    (int)smem_));
+    } else if (kb_ == 2) {
+      smem_ = TcLayout<2, 128, false>::kBytes + 1024;
+      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<2, 128, 16, false>, (cudaFuncAttribute)attr,
+                                    (int)smem_));
     } else {
-      epi_ = 8;  // 64-chain tiles: 32 chains per epilogue warp
-      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<4, 64, 8>, (cudaFuncAttribute)attr, (int)smem_));
+      smem_ = TcLayout<4, 64, false>::kBytes + 1024;
+      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<4, 64, 8, false>, (cudaFuncAttribute)attr,
+                                    (int)smem_));
     }
   }
 
@@ -544,14 +580,12 @@ class LogregTc final : public Target {
     double* lpart = static_cast<double*>(ws);
     float* gpart = reinterpret_cast<float*>(lpart + rows);
     const int N = (int)N_, D = (int)D_;
-#define GBM_TC_LAUNCH(KB_, CT_, EPI_)                                                     \
-  logreg_tc_kernel<KB_, CT_, EPI_><<<grid_, tc_threads(EPI_), smem_, s>>>(                \
-      xmap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_dev_)
-    if (kb_ == 2) {
-      if (epi_ == 8) GBM_TC_LAUNCH(2, 128, 8); else GBM_TC_LAUNCH(2, 128, 16);
-    } else {
-      GBM_TC_LAUNCH(4, 64, 8);
-    }
+#define GBM_TC_LAUNCH(KB_, CT_, EPI_, XLO_)                                               \
+  logreg_tc_kernel<KB_, CT_, EPI_, XLO_><<<grid_, tc_threads(EPI_), smem_, s>>>(          \
+      xmap_, xlomap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_dev_)
+    if (kb_ == 2 && xlo_) GBM_TC_LAUNCH(2, 128, 16, true);
+    else if (kb_ == 2) GBM_TC_LAUNCH(2, 128, 16, false);
+    else GBM_TC_LAUNCH(4, 64, 8, false);
 #undef GBM_TC_LAUNCH
     GBM_CUDA(cudaGetLastError());
     tc_reduce_kernel<<<(cap + 7) / 8, 256, 0, s>>>(lpart, gpart, q, ldq, n_dev, ct_, grid_, N, D,
@@ -567,11 +601,27 @@ class LogregTc final : public Target {
 
  private:
   int64_t N_, D_;
-  int kb_ = 2, ct_ = 128, grid_ = 0, epi_ = 16;
+  int kb_ = 2, ct_ = 128, grid_ = 0;
   size_t smem_ = 0;
   float inv_var_ = 1.f;
   double log_norm_ = 0.0;
-  DeviceBuffer xb_, y_;
+  // Tensor map over a BF16 [N][Dp] matrix: boxes of 64 features x 128 rows,
+  // 128-byte swizzle, rows past N read as zeros.
+  void encode(CUtensorMap* map, void* base, int Dp) {
+    cuuint64_t dims[2] = {(cuuint64_t)Dp, (cuuint64_t)N_};
+    cuuint64_t strides[1] = {(cuuint64_t)Dp * 2};
+    cuuint32_t box[2] = {64, (cuuint32_t)kRows};
+    cuuint32_t estr[2] = {1, 1};
+    CUresult r = encode_tiled()(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides,
+                                box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                                CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                                CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) throw CudaError{cudaErrorInvalidValue, "cuTensorMapEncodeTiled"};
+  }
+
+  DeviceBuffer xb_, xl_, y_;
+  bool xlo_ = false;
+  CUtensorMap xlomap_;
   int* err_dev_ = nullptr;
   CUtensorMap xmap_;
 };

@@ -45,6 +45,21 @@ def test_mixed_log_prob_and_grad_vs_fp64(pg, n, d, c):
   np.testing.assert_allclose(g.cpu().numpy(), g_o, rtol=0, atol=1e-3 * scale)
 
 
+@pytest.mark.parametrize('n,d,c', [(5000, 100, 300), (1000, 25, 64), (257, 128, 129)])
+def test_mixed_on_fp32_data_keeps_fp32_fidelity(pg, n, d, c):
+  """FP32 X (up to 128 features) is kept as BF16 hi + lo; the log-density is
+  then that of the FP32 data, not of X rounded to BF16."""
+  X, y, _ = _problems.logreg_data(n, d, seed=2 * n + d, scale=1.0 / np.sqrt(d))
+  t = pg.LogisticRegression(X, y, precision='mixed')
+  o = otargets.LogisticRegression(X, y)
+  q = (np.random.default_rng(c).normal(size=(c, d)) * 0.5).astype(np.float32)
+  lp, g = t.log_prob_and_grad(torch.from_numpy(q).cuda())
+  lp_o, g_o = o(q)
+  np.testing.assert_allclose(lp.cpu().numpy(), lp_o, rtol=1e-5, atol=1e-2)
+  scale = np.abs(g_o).max()
+  np.testing.assert_allclose(g.cpu().numpy(), g_o, rtol=0, atol=2e-3 * scale)
+
+
 def test_mixed_matches_fp32_target_on_same_data(pg):
   X, y, _ = _problems.logreg_data(3000, 100, seed=3, scale=0.1)
   Xr = _bf16_round(X)
