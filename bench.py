@@ -37,7 +37,10 @@ WORKLOADS = {
                                 feature_scale=0.1, step0=0.1, target_accept=0.8,
                                 num_adaptation_steps=1000, precision='mixed'),
 }
+WORKLOADS['hmc_logreg_1000x25'] = dict(n=1000, d=25, chains=64, seed=0, feature_scale=1.0,
+                                       step0=0.03, leapfrogs=10, burnin=500, precision='fp32')
 METRIC = 'grad-evals/s (NUTS leapfrogs_taken summed over chains; min-ESS/s reported beside)'
+METRIC_HMC = 'grad-evals/s (HMC: chains x num_leapfrog_steps per transition; min-ESS/s beside)'
 
 
 def make_data(w):
@@ -213,6 +216,45 @@ def run_kernel_only(args, w):
   flops, nbytes = target.cost(q.shape[0])
   print(json.dumps({'kernel_only': True, 'precision': target.precision, 'ms_per_eval': ms,
                     'tflops': flops / ms / 1e9, 'chains': q.shape[0]}), flush=True)
+
+
+def run_hmc(args, w):
+  """HMC on the 1000 x 25 logistic regression (64 chains, step 0.03, 10
+  leapfrog steps): burn-in untimed, then K transitions timed through the
+  device-resident chain loop."""
+  import torch
+  import probability_gb300 as pg
+  X, y, init = make_data(w)
+  target = pg.LogisticRegression(X, y, precision=args.precision or w['precision'])
+  k = pg.mcmc.HamiltonianMonteCarlo(target, step_size=w['step0'],
+                                    num_leapfrog_steps=w['leapfrogs'])
+  q = torch.from_numpy(init).cuda()
+  run = pg.mcmc.run_chain(k, 1, q, num_burnin_steps=w['burnin'] + args.warmup - 1,
+                          seed=(w['seed'], 0))
+  q = run.final_state
+  first = w['burnin'] + args.warmup
+  torch.cuda.synchronize()
+  e0 = torch.cuda.Event(enable_timing=True)
+  e1 = torch.cuda.Event(enable_timing=True)
+  e0.record()
+  run = pg.mcmc.run_chain(k, args.steps, q, seed=(w['seed'], 0), first_step=first)
+  e1.record()
+  e1.synchronize()
+  secs = e0.elapsed_time(e1) / 1000.0
+  evals = args.steps * w['chains'] * w['leapfrogs']
+  ess = pg.mcmc.effective_sample_size(run.all_states, filter_beyond_positive_pairs=True,
+                                      cross_chain_dims=1)
+  acc = run.trace['is_accepted'].float().mean().item()
+  print(json.dumps({
+      'metric': METRIC_HMC, 'value': evals / secs, 'unit': 'grad-evals/s', 'n_gpus': 1,
+      'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1000 * secs / args.steps,
+      'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
+      'data': 'synthetic (seeded numpy default_rng(0))',
+      'config': {'workload': 'hmc_logreg_1000x25', 'rows': w['n'], 'features': w['d'],
+                 'chains': w['chains'], 'step_size': w['step0'],
+                 'num_leapfrog_steps': w['leapfrogs'], 'burnin': w['burnin'],
+                 'precision': target.precision, 'l2': 'inputs L2-resident (100 KB of X)'},
+      'min_ess_per_s': float(ess.min().item()) / secs, 'accept_rate': acc}), flush=True)
 
 
 def run_engine(args, w):
@@ -454,6 +496,8 @@ def main():
     run_reference(args, w)
   elif args.kernel_only:
     run_kernel_only(args, w)
+  elif args.workload.startswith('hmc_'):
+    run_hmc(args, w)
   else:
     run_engine(args, w)
 

@@ -83,6 +83,26 @@ GBM_API int gbm_step_key(const uint32_t seed[2], uint64_t step, uint32_t out[2])
 GBM_API int gbm_target_logistic_regression(gbm_context* ctx, const void* x, int x_dtype,
                                    int64_t num_rows, int64_t num_features, const float* y,
                                    float prior_scale, int precision, gbm_target** out);
+/* Multivariate normal MultivariateNormalTriL(loc, L) (distributions/
+ * mvn_tril.py:44, mvn_linear_operator.py:242): loc [dim] and the inverse
+ * scale factor L^-1 [dim][dim] (row-major, lower triangular, float32):
+ * u = L^-1 (x - loc), logp = -1/2 |u|^2 + log_normalizer, grad = -L^-T u,
+ * with log_normalizer = -sum log|L_ii| - dim/2 log 2pi supplied by the
+ * caller. */
+GBM_API int gbm_target_mvn(gbm_context* ctx, const float* loc, const float* scale_tril_inv,
+                           int64_t dim, double log_normalizer, gbm_target** out);
+
+/* Non-centred hierarchical normal (the eight-schools model of
+ * mcmc/eight_schools_hmc.py:41-58): mu ~ N(0, mu_scale), tau ~
+ * HalfCauchy(0, tau_scale), z_j ~ N(0, 1), y_j ~ N(mu + tau z_j, sigma_j),
+ * j < groups.  State [mu, log tau, z_1..z_groups] (dim = groups + 2); the
+ * log-density includes the log-Jacobian of tau = exp(log tau), as
+ * TransformedTransitionKernel with an Exp bijector gives
+ * (mcmc/transformed_kernel.py:165).  y, sigma: float32 [groups]. */
+GBM_API int gbm_target_hierarchical_normal(gbm_context* ctx, const float* y, const float* sigma,
+                                           int64_t groups, float mu_scale, float tau_scale,
+                                           gbm_target** out);
+
 GBM_API int gbm_target_destroy(gbm_target* target);
 GBM_API int gbm_target_dim(const gbm_target* target, int64_t* dim);
 
@@ -176,6 +196,46 @@ GBM_API int gbm_nuts_last_leaf_iterations(const gbm_nuts* kernel, int64_t* out);
 GBM_API int gbm_nuts_set_profiling(gbm_nuts* kernel, int enable);
 GBM_API int gbm_nuts_read_profile(gbm_nuts* kernel, double* eval_ms, int64_t* evals,
                                   int64_t* kernel_launches);
+
+/* ---- sample_chain ------------------------------------------------------- */
+
+/* sample_chain (mcmc/sample.py:81-383) over NoUTurnSampler, optionally inside
+ * DualAveragingStepSizeAdaptation, run entirely on the device: result 0
+ * after 1 + num_burnin_steps transitions, then one result every
+ * 1 + num_steps_between_results.  Transition t uses gbm_step_key(seed,
+ * first_step + t).  state/target_log_prob/grads (in: current, out: final)
+ * and step_size (float32 [1] or [chains]; in: next step size, out: final)
+ * are updated in place.  num_adaptation_steps <= 0 disables adaptation;
+ * otherwise da_state is the float64 [groups][4] dual-averaging state of
+ * gbm_dual_averaging_update (in/out).  Trace pointers ([num_results][...],
+ * device) may each be NULL.  Blocks the host at most once per tree depth
+ * per transition. */
+GBM_API int gbm_nuts_sample_chain(gbm_nuts* kernel, int64_t chains, float* state,
+                                  double* target_log_prob, float* grads_target_log_prob,
+                                  float* step_size, int step_size_per_chain,
+                                  const uint32_t seed[2], int64_t first_step,
+                                  int64_t num_results, int64_t num_burnin_steps,
+                                  int64_t num_steps_between_results,
+                                  int32_t num_adaptation_steps, double target_accept_prob,
+                                  double exploration_shrinkage, double step_count_smoothing,
+                                  double decay_rate, double* da_state, float* trace_state,
+                                  double* trace_target_log_prob, double* trace_log_accept_ratio,
+                                  int32_t* trace_leapfrogs_taken, uint8_t* trace_is_accepted,
+                                  uint8_t* trace_has_divergence, float* trace_step_size);
+
+/* The same loop over MetropolisHastings(UncalibratedHamiltonianMonteCarlo)
+ * with num_leapfrog_steps leapfrog steps per transition; fully asynchronous. */
+GBM_API int gbm_hmc_sample_chain(gbm_hmc* kernel, int64_t chains, float* state,
+                                 double* target_log_prob, float* grads_target_log_prob,
+                                 float* step_size, int step_size_per_chain,
+                                 int32_t num_leapfrog_steps, const uint32_t seed[2],
+                                 int64_t first_step, int64_t num_results,
+                                 int64_t num_burnin_steps, int64_t num_steps_between_results,
+                                 int32_t num_adaptation_steps, double target_accept_prob,
+                                 double exploration_shrinkage, double step_count_smoothing,
+                                 double decay_rate, double* da_state, float* trace_state,
+                                 double* trace_target_log_prob, double* trace_log_accept_ratio,
+                                 uint8_t* trace_is_accepted, float* trace_step_size);
 
 /* ---- DualAveragingStepSizeAdaptation ----------------------------------- */
 

@@ -3,6 +3,8 @@ HamiltonianMonteCarlo, NoUTurnSampler, DualAveragingStepSizeAdaptation and
 sample_chain, with hand-written sm_103a kernels behind a C ABI
 (include/gb300_mcmc.h)."""
 from probability_gb300 import mcmc, targets
-from probability_gb300.targets import LogisticRegression
+from probability_gb300.targets import (LogisticRegression, MultivariateNormalTriL,
+                                       NonCentredHierarchicalNormal)
 
-__all__ = ['mcmc', 'targets', 'LogisticRegression']
+__all__ = ['mcmc', 'targets', 'LogisticRegression', 'MultivariateNormalTriL',
+           'NonCentredHierarchicalNormal']

@@ -42,6 +42,9 @@ _SIGNATURES = {
     'gbm_target_logistic_regression': (
         [P, P, ctypes.c_int, I64, I64, P, F32, ctypes.c_int, ctypes.POINTER(P)], ctypes.c_int),
     'gbm_target_destroy': ([P], ctypes.c_int),
+    'gbm_target_mvn': ([P, P, P, I64, F64, ctypes.POINTER(P)], ctypes.c_int),
+    'gbm_target_hierarchical_normal': ([P, P, P, I64, F32, F32, ctypes.POINTER(P)],
+                                       ctypes.c_int),
     'gbm_target_dim': ([P, ctypes.POINTER(I64)], ctypes.c_int),
     'gbm_target_log_prob_and_grad': ([P, P, I64, P, P], ctypes.c_int),
     'gbm_target_cost': ([P, I64, ctypes.POINTER(F64), ctypes.POINTER(F64)], ctypes.c_int),
@@ -58,6 +61,10 @@ _SIGNATURES = {
     'gbm_dual_averaging_update': (
         [P, I64, P, ctypes.c_int, I32, F64, P, F64, F64, F64, P, P], ctypes.c_int),
     'gbm_step_key': ([U32P, ctypes.c_uint64, U32P], ctypes.c_int),
+    'gbm_nuts_sample_chain': ([P, I64, P, P, P, P, ctypes.c_int, U32P, I64, I64, I64, I64, I32,
+                               F64, F64, F64, F64] + [P] * 8, ctypes.c_int),
+    'gbm_hmc_sample_chain': ([P, I64, P, P, P, P, ctypes.c_int, I32, U32P, I64, I64, I64, I64,
+                              I32, F64, F64, F64, F64] + [P] * 6, ctypes.c_int),
     'gbm_logreg_log_prob_and_grad_noalloc': ([P, I64, I64, P, F32, P, I64, P, P, P],
                                              ctypes.c_int),
 }

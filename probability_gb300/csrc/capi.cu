@@ -173,6 +173,47 @@ int gbm_target_logistic_regression(gbm_context* ctx, const void* x, int x_dtype,
   });
 }
 
+static int finish_target(gbm_context* ctx, gbm_target* t, gbm_target** out) {
+  GBM_CUDA(cudaMalloc(&t->count.ptr, sizeof(int)));
+  t->count.bytes = sizeof(int);
+  GBM_CUDA(cudaStreamSynchronize(ctx->stream));
+  *out = t;
+  return GBM_OK;
+}
+
+int gbm_target_mvn(gbm_context* ctx, const float* loc, const float* precision, int64_t dim,
+                   double log_normalizer, gbm_target** out) {
+  if (!ctx || !loc || !precision || !out) return invalid("gbm_target_mvn: NULL argument");
+  if (dim <= 0 || dim > 65536) return invalid("gbm_target_mvn: dim must be in [1, 65536]");
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    std::unique_ptr<gbm_target> t(new gbm_target());
+    t->ctx = ctx;
+    t->impl = gbm::make_mvn(ctx, loc, precision, dim, log_normalizer);
+    finish_target(ctx, t.get(), out);
+    t.release();
+    return GBM_OK;
+  });
+}
+
+int gbm_target_hierarchical_normal(gbm_context* ctx, const float* y, const float* sigma,
+                                   int64_t groups, float mu_scale, float tau_scale,
+                                   gbm_target** out) {
+  if (!ctx || !y || !sigma || !out) return invalid("gbm_target_hierarchical_normal: NULL argument");
+  if (groups <= 0 || groups > (1 << 24)) return invalid("gbm_target_hierarchical_normal: bad groups");
+  if (!(mu_scale > 0.f) || !(tau_scale > 0.f))
+    return invalid("gbm_target_hierarchical_normal: scales must be > 0");
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    std::unique_ptr<gbm_target> t(new gbm_target());
+    t->ctx = ctx;
+    t->impl = gbm::make_hier(ctx, y, sigma, groups, mu_scale, tau_scale);
+    finish_target(ctx, t.get(), out);
+    t.release();
+    return GBM_OK;
+  });
+}
+
 int gbm_target_destroy(gbm_target* t) {
   if (!t) return GBM_OK;
   return guarded([&] {
@@ -225,6 +266,7 @@ int gbm_hmc_create(gbm_target* target, int64_t max_chains, gbm_hmc** out) {
     DeviceGuard g(target->ctx->device);
     auto* k = new gbm_hmc();
     k->target = target;
+    k->ctx = target->ctx;
     k->max_chains = max_chains;
     try {
       gbm::hmc_setup(k);
@@ -240,8 +282,9 @@ int gbm_hmc_create(gbm_target* target, int64_t max_chains, gbm_hmc** out) {
 int gbm_hmc_destroy(gbm_hmc* k) {
   if (!k) return GBM_OK;
   return guarded([&] {
-    DeviceGuard g(k->target->ctx->device);
-    cudaStreamSynchronize(k->target->ctx->stream);
+    // Uses only the handle's own context: the target may already be gone.
+    DeviceGuard g(k->ctx->device);
+    cudaStreamSynchronize(k->ctx->stream);
     delete k;
     return GBM_OK;
   });
@@ -285,6 +328,7 @@ int gbm_nuts_create(gbm_target* target, int64_t max_chains, int32_t max_tree_dep
     DeviceGuard g(target->ctx->device);
     auto* k = new gbm_nuts();
     k->target = target;
+    k->ctx = target->ctx;
     k->max_chains = max_chains;
     k->max_tree_depth = max_tree_depth;
     k->max_energy_diff = max_energy_diff;
@@ -303,8 +347,9 @@ int gbm_nuts_create(gbm_target* target, int64_t max_chains, int32_t max_tree_dep
 int gbm_nuts_destroy(gbm_nuts* k) {
   if (!k) return GBM_OK;
   return guarded([&] {
-    DeviceGuard g(k->target->ctx->device);
-    cudaStreamSynchronize(k->target->ctx->stream);
+    // Uses only the handle's own context: the target may already be gone.
+    DeviceGuard g(k->ctx->device);
+    cudaStreamSynchronize(k->ctx->stream);
     for (auto& ev : k->poll_events)
       if (ev) cudaEventDestroy(ev);
     for (auto& ev : k->prof_events) cudaEventDestroy(ev);
@@ -340,6 +385,77 @@ int gbm_nuts_last_leaf_iterations(const gbm_nuts* k, int64_t* out) {
   if (!k || !out) return invalid("gbm_nuts_last_leaf_iterations: NULL argument");
   *out = k->last_leaf_iterations;
   return GBM_OK;
+}
+
+static int check_loop_args(int64_t chains, int64_t max_chains, int64_t first_step,
+                           int64_t num_results, int64_t burnin, int64_t thin,
+                           int32_t num_adaptation_steps, const double* da_state) {
+  if (chains <= 0 || chains > max_chains) return invalid("sample_chain: chains must be in [1, max_chains]");
+  if (num_results < 1 || burnin < 0 || thin < 0 || first_step < 0)
+    return invalid("sample_chain: need num_results >= 1, burn-in, thinning, first_step >= 0");
+  const int64_t total = first_step + burnin + 1 + (num_results - 1) * (1 + thin);
+  if (total >= ((int64_t)1 << 32)) return invalid("sample_chain: more than 2^32 transitions");
+  if (num_adaptation_steps > 0 && !da_state)
+    return invalid("sample_chain: adaptation needs da_state");
+  return GBM_OK;
+}
+
+int gbm_nuts_sample_chain(gbm_nuts* k, int64_t chains, float* state, double* tlp, float* grads,
+                          float* step_size, int per_chain, const uint32_t seed[2],
+                          int64_t first_step, int64_t num_results, int64_t burnin, int64_t thin,
+                          int32_t num_adaptation_steps, double target_accept_prob,
+                          double exploration_shrinkage, double step_count_smoothing,
+                          double decay_rate, double* da_state, float* trace_state,
+                          double* trace_tlp, double* trace_lar, int32_t* trace_lf,
+                          uint8_t* trace_acc, uint8_t* trace_div, float* trace_eps) {
+  if (!k || !state || !tlp || !grads || !step_size || !seed)
+    return invalid("gbm_nuts_sample_chain: NULL argument");
+  const int st = check_loop_args(chains, k->max_chains, first_step, num_results, burnin, thin,
+                                 num_adaptation_steps, da_state);
+  if (st != GBM_OK) return st;
+  return guarded([&] {
+    DeviceGuard g(k->target->ctx->device);
+    gbm::check_device_error(k->target->ctx);
+    gbm::DaConfig da{num_adaptation_steps > 0 ? 1 : 0,
+                     gbm::DaParams{target_accept_prob, exploration_shrinkage,
+                                   step_count_smoothing, decay_rate, num_adaptation_steps},
+                     nullptr, da_state};
+    gbm::ChainTrace tr{trace_state, trace_tlp, trace_lar, trace_lf, trace_acc, trace_div,
+                       trace_eps};
+    gbm::nuts_sample_chain(k, chains, state, tlp, grads, step_size, per_chain,
+                           make_uint2(seed[0], seed[1]), (uint32_t)first_step, num_results,
+                           burnin, thin, da, tr);
+    return GBM_OK;
+  });
+}
+
+int gbm_hmc_sample_chain(gbm_hmc* k, int64_t chains, float* state, double* tlp, float* grads,
+                         float* step_size, int per_chain, int32_t num_leapfrog_steps,
+                         const uint32_t seed[2], int64_t first_step, int64_t num_results,
+                         int64_t burnin, int64_t thin, int32_t num_adaptation_steps,
+                         double target_accept_prob, double exploration_shrinkage,
+                         double step_count_smoothing, double decay_rate, double* da_state,
+                         float* trace_state, double* trace_tlp, double* trace_lar,
+                         uint8_t* trace_acc, float* trace_eps) {
+  if (!k || !state || !tlp || !grads || !step_size || !seed)
+    return invalid("gbm_hmc_sample_chain: NULL argument");
+  if (num_leapfrog_steps < 1) return invalid("gbm_hmc_sample_chain: num_leapfrog_steps < 1");
+  const int st = check_loop_args(chains, k->max_chains, first_step, num_results, burnin, thin,
+                                 num_adaptation_steps, da_state);
+  if (st != GBM_OK) return st;
+  return guarded([&] {
+    DeviceGuard g(k->target->ctx->device);
+    gbm::check_device_error(k->target->ctx);
+    gbm::DaConfig da{num_adaptation_steps > 0 ? 1 : 0,
+                     gbm::DaParams{target_accept_prob, exploration_shrinkage,
+                                   step_count_smoothing, decay_rate, num_adaptation_steps},
+                     nullptr, da_state};
+    gbm::ChainTrace tr{trace_state, trace_tlp, trace_lar, nullptr, trace_acc, nullptr, trace_eps};
+    gbm::hmc_sample_chain(k, chains, state, tlp, grads, step_size, per_chain, num_leapfrog_steps,
+                          make_uint2(seed[0], seed[1]), (uint32_t)first_step, num_results, burnin,
+                          thin, da, tr);
+    return GBM_OK;
+  });
 }
 
 int gbm_nuts_set_profiling(gbm_nuts* k, int enable) {

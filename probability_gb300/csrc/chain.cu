@@ -1,0 +1,130 @@
+// Device-resident sample_chain loops (mcmc/sample.py:311-383): burn-in,
+// thinning, optional dual-averaging step-size adaptation
+// (mcmc/dual_averaging_step_size_adaptation.py:477-532) and the trace, all
+// enqueued on the context stream from C++ -- no host language in the loop.
+// Transition t uses the key step_key(seed, first_step + t), so a run split
+// into several calls (first_step advancing) draws exactly as one long run.
+#include <cuda_runtime.h>
+
+#include <utility>
+
+#include "rng.cuh"
+#include "samplers.h"
+
+namespace gbm {
+
+namespace {
+
+template <class T>
+void copy_row(T* dst, const T* src, size_t n, cudaStream_t s) {
+  if (dst) GBM_CUDA(cudaMemcpyAsync(dst, src, n * sizeof(T), cudaMemcpyDeviceToDevice, s));
+}
+
+// Ping-pong state buffers plus per-transition result buffers for C chains.
+struct LoopBuffers {
+  float *q, *g;
+  double *l, *lar, *energy, *corr;
+  int32_t* lf;
+  uint8_t *acc, *rmd, *div;
+};
+
+LoopBuffers carve(DeviceBuffer& mem, int64_t C, int64_t D) {
+  const size_t vec = (size_t)C * D;
+  size_t bytes = 0;
+  auto take = [&](size_t b) { size_t at = bytes; bytes += (b + 255) / 256 * 256; return at; };
+  const size_t oq = take(4 * vec), og = take(4 * vec), ol = take(8 * C), olar = take(8 * C);
+  const size_t oe = take(8 * C), oc = take(8 * C), olf = take(4 * C), oa = take(C), orm = take(C),
+               od = take(C);
+  mem.reserve(bytes);
+  char* b = mem.as<char>();
+  LoopBuffers r;
+  r.q = reinterpret_cast<float*>(b + oq);
+  r.g = reinterpret_cast<float*>(b + og);
+  r.l = reinterpret_cast<double*>(b + ol);
+  r.lar = reinterpret_cast<double*>(b + olar);
+  r.energy = reinterpret_cast<double*>(b + oe);
+  r.corr = reinterpret_cast<double*>(b + oc);
+  r.lf = reinterpret_cast<int32_t*>(b + olf);
+  r.acc = reinterpret_cast<uint8_t*>(b + oa);
+  r.rmd = reinterpret_cast<uint8_t*>(b + orm);
+  r.div = reinterpret_cast<uint8_t*>(b + od);
+  return r;
+}
+
+}  // namespace
+
+void nuts_sample_chain(gbm_nuts* k, int64_t C, float* q, double* l, float* g, float* eps,
+                       int per_chain, uint2 seed, uint32_t first_step, int64_t num_results,
+                       int64_t burnin, int64_t thin, const DaConfig& da, const ChainTrace& tr) {
+  cudaStream_t s = k->target->ctx->stream;
+  const int64_t D = k->target->impl->dim;
+  const size_t vec = (size_t)C * D;
+  LoopBuffers b = carve(k->loop_mem, C, D);
+  float *cq = q, *cg = g, *nq = b.q, *ng = b.g;
+  double *cl = l, *nl = b.l;
+  const int64_t groups = per_chain ? C : 1;
+  uint32_t t = first_step;
+  for (int64_t r = 0; r < num_results; ++r) {
+    const int64_t n = (r == 0) ? 1 + burnin : 1 + thin;
+    for (int64_t i = 0; i < n; ++i, ++t) {
+      NutsOutputs out{nq, nl, ng, b.lar, b.lf, b.acc, b.rmd, b.div, b.energy, nullptr};
+      nuts_one_step(k, C, cq, cl, cg, eps, per_chain, step_key(seed, t), out);
+      if (da.enabled)
+        dual_averaging_update(s, b.lar, C, per_chain, da.prm, da.target_accept, da.state, eps);
+      std::swap(cq, nq);
+      std::swap(cl, nl);
+      std::swap(cg, ng);
+    }
+    copy_row(tr.state ? tr.state + r * vec : nullptr, cq, vec, s);
+    copy_row(tr.target_log_prob ? tr.target_log_prob + r * C : nullptr, cl, C, s);
+    copy_row(tr.log_accept_ratio ? tr.log_accept_ratio + r * C : nullptr, b.lar, C, s);
+    copy_row(tr.leapfrogs_taken ? tr.leapfrogs_taken + r * C : nullptr, b.lf, C, s);
+    copy_row(tr.is_accepted ? tr.is_accepted + r * C : nullptr, b.acc, C, s);
+    copy_row(tr.has_divergence ? tr.has_divergence + r * C : nullptr, b.div, C, s);
+    copy_row(tr.step_size ? tr.step_size + r * groups : nullptr, eps, groups, s);
+  }
+  if (cq != q) {  // the final state lives in the scratch buffers: hand it back
+    copy_row(q, cq, vec, s);
+    copy_row(g, cg, vec, s);
+    copy_row(l, cl, C, s);
+  }
+}
+
+void hmc_sample_chain(gbm_hmc* k, int64_t C, float* q, double* l, float* g, float* eps,
+                      int per_chain, int num_leapfrog_steps, uint2 seed, uint32_t first_step,
+                      int64_t num_results, int64_t burnin, int64_t thin, const DaConfig& da,
+                      const ChainTrace& tr) {
+  cudaStream_t s = k->target->ctx->stream;
+  const int64_t D = k->target->impl->dim;
+  const size_t vec = (size_t)C * D;
+  LoopBuffers b = carve(k->loop_mem, C, D);
+  float *cq = q, *cg = g, *nq = b.q, *ng = b.g;
+  double *cl = l, *nl = b.l;
+  const int64_t groups = per_chain ? C : 1;
+  uint32_t t = first_step;
+  for (int64_t r = 0; r < num_results; ++r) {
+    const int64_t n = (r == 0) ? 1 + burnin : 1 + thin;
+    for (int64_t i = 0; i < n; ++i, ++t) {
+      HmcOutputs out{nq, nl, ng, nullptr, nullptr, nullptr, nullptr, nullptr,
+                     b.corr, b.lar, b.acc};
+      hmc_one_step(k, C, cq, cl, cg, eps, per_chain, num_leapfrog_steps, step_key(seed, t), out);
+      if (da.enabled)
+        dual_averaging_update(s, b.lar, C, per_chain, da.prm, da.target_accept, da.state, eps);
+      std::swap(cq, nq);
+      std::swap(cl, nl);
+      std::swap(cg, ng);
+    }
+    copy_row(tr.state ? tr.state + r * vec : nullptr, cq, vec, s);
+    copy_row(tr.target_log_prob ? tr.target_log_prob + r * C : nullptr, cl, C, s);
+    copy_row(tr.log_accept_ratio ? tr.log_accept_ratio + r * C : nullptr, b.lar, C, s);
+    copy_row(tr.is_accepted ? tr.is_accepted + r * C : nullptr, b.acc, C, s);
+    copy_row(tr.step_size ? tr.step_size + r * groups : nullptr, eps, groups, s);
+  }
+  if (cq != q) {
+    copy_row(q, cq, vec, s);
+    copy_row(g, cg, vec, s);
+    copy_row(l, cl, C, s);
+  }
+}
+
+}  // namespace gbm

@@ -76,6 +76,11 @@ inline void check_device_error(gbm_context* ctx) {
 // Write the batch-size word `*count = n` on stream `s` (no host memory).
 void set_count(int* count, int n, cudaStream_t s);
 
+std::unique_ptr<Target> make_mvn(gbm_context* ctx, const float* loc, const float* scale_tril_inv,
+                                 int64_t d, double log_norm);
+std::unique_ptr<Target> make_hier(gbm_context* ctx, const float* y, const float* sigma, int64_t J,
+                                  float mu_scale, float tau_scale);
+
 std::unique_ptr<Target> make_logreg_simt(gbm_context* ctx, const float* X, int64_t n,
                                          int64_t d, const float* y, float prior_scale);
 

@@ -70,6 +70,25 @@ struct DaParams {
   int num_adaptation_steps;
 };
 
+// Traced outputs of a device-resident chain loop; any pointer may be NULL.
+struct ChainTrace {
+  float* state;               // [R][C][D]
+  double* target_log_prob;    // [R][C]
+  double* log_accept_ratio;   // [R][C]
+  int32_t* leapfrogs_taken;   // [R][C] (NUTS)
+  uint8_t* is_accepted;       // [R][C]
+  uint8_t* has_divergence;    // [R][C] (NUTS)
+  float* step_size;           // [R][groups]
+};
+
+// Dual-averaging configuration of a chain loop (enabled = 0: fixed step).
+struct DaConfig {
+  int enabled;
+  DaParams prm;
+  const double* target_accept;  // [groups] or NULL
+  double* state;                // [groups][4]
+};
+
 }  // namespace gbm
 
 struct gbm_nuts;
@@ -86,10 +105,18 @@ void hmc_one_step(gbm_hmc* k, int64_t chains, const float* q, const double* l, c
 void dual_averaging_update(cudaStream_t s, const double* lar, int64_t C, int per_chain,
                            const DaParams& prm, const double* target_accept, double* state,
                            float* eps);
+void nuts_sample_chain(gbm_nuts* k, int64_t C, float* q, double* l, float* g, float* eps,
+                       int per_chain, uint2 seed, uint32_t first_step, int64_t num_results,
+                       int64_t burnin, int64_t thin, const DaConfig& da, const ChainTrace& tr);
+void hmc_sample_chain(gbm_hmc* k, int64_t C, float* q, double* l, float* g, float* eps,
+                      int per_chain, int num_leapfrog_steps, uint2 seed, uint32_t first_step,
+                      int64_t num_results, int64_t burnin, int64_t thin, const DaConfig& da,
+                      const ChainTrace& tr);
 }  // namespace gbm
 
 struct gbm_nuts {
-  gbm_target* target = nullptr;
+  gbm_target* target = nullptr;   // must outlive every call except destroy
+  gbm_context* ctx = nullptr;
   int64_t max_chains = 0;
   int max_tree_depth = 10;
   double max_energy_diff = 1000.0;
@@ -98,6 +125,7 @@ struct gbm_nuts {
   std::vector<int> read_lo, read_hi;        // per leaf
   gbm::DeviceBuffer mem;
   gbm::DeviceBuffer target_ws;
+  gbm::DeviceBuffer loop_mem;   // chain-loop ping-pong and result buffers
   gbm::NutsDev dev{};
   cudaEvent_t poll_events[4] = {nullptr, nullptr, nullptr, nullptr};
   // Counters for the last transition (host-visible after one_step returns).
@@ -116,8 +144,10 @@ void nuts_profile_flush(gbm_nuts* k);  // stream must be synchronized
 }  // namespace gbm
 
 struct gbm_hmc {
-  gbm_target* target = nullptr;
+  gbm_target* target = nullptr;   // must outlive every call except destroy
+  gbm_context* ctx = nullptr;
   int64_t max_chains = 0;
   gbm::DeviceBuffer mem;
   gbm::DeviceBuffer target_ws;
+  gbm::DeviceBuffer loop_mem;   // chain-loop ping-pong and result buffers
 };

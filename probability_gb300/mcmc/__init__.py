@@ -7,14 +7,14 @@ from probability_gb300.mcmc.hmc import (HamiltonianMonteCarlo, UncalibratedHamil
 from probability_gb300.mcmc.kernel import TransitionKernel
 from probability_gb300.mcmc.metropolis_hastings import MetropolisHastingsKernelResults
 from probability_gb300.mcmc.nuts import NoUTurnSampler, NUTSKernelResults
-from probability_gb300.mcmc.sample import (CheckpointableStatesAndTrace, StatesAndTrace,
-                                           sample_chain)
+from probability_gb300.mcmc.sample import (ChainRun, CheckpointableStatesAndTrace,
+                                           StatesAndTrace, run_chain, sample_chain)
 from probability_gb300.mcmc.simple_step_size_adaptation import (
     hmc_like_log_accept_prob_getter_fn, hmc_like_step_size_getter_fn,
     hmc_like_step_size_setter_fn)
 
 __all__ = [
-    'CheckpointableStatesAndTrace', 'DualAveragingStepSizeAdaptation',
+    'ChainRun', 'run_chain', 'CheckpointableStatesAndTrace', 'DualAveragingStepSizeAdaptation',
     'DualAveragingStepSizeAdaptationResults', 'HamiltonianMonteCarlo',
     'MetropolisHastingsKernelResults', 'NUTSKernelResults', 'NoUTurnSampler', 'StatesAndTrace',
     'TransitionKernel', 'UncalibratedHamiltonianMonteCarlo',

@@ -102,6 +102,54 @@ class LogisticRegression(Target):
     self._ctx = ctx
 
 
+class MultivariateNormalTriL(Target):
+  """MultivariateNormalTriL(loc, scale_tril) (distributions/mvn_tril.py:44).
+
+  L^-1 and the normalizer are formed once, in float64, at construction; the
+  batched log-density -1/2 |L^-1 (x - loc)|^2 and gradient -L^-T L^-1 (x - loc)
+  run on the device.
+  """
+
+  def __init__(self, loc, scale_tril):
+    L = np.asarray(_util.as_tensor(scale_tril, torch.float64).cpu().numpy(), np.float64)
+    mu = np.asarray(_util.as_tensor(loc, torch.float64).cpu().numpy(), np.float64).reshape(-1)
+    d = L.shape[-1]
+    if L.shape != (d, d) or mu.shape[0] != d:
+      raise ValueError('scale_tril must be [D, D] and loc [D]')
+    import scipy.linalg
+    Linv = scipy.linalg.solve_triangular(np.tril(L), np.eye(d), lower=True)
+    log_norm = -np.sum(np.log(np.abs(np.diag(L)))) - 0.5 * d * np.log(2 * np.pi)
+    self.loc = mu
+    ctx = _native.Context.current()
+    loc_t = _util.as_tensor(mu, torch.float32)
+    linv_t = _util.as_tensor(np.tril(Linv), torch.float32)
+    h = ctypes.c_void_p()
+    _native.check(_native.lib().gbm_target_mvn(ctx.handle, _native.ptr(loc_t), _native.ptr(linv_t),
+                                               d, float(log_norm), ctypes.byref(h)),
+                  'gbm_target_mvn')
+    self._handle = h
+    self._ctx = ctx
+
+
+class NonCentredHierarchicalNormal(Target):
+  """Non-centred hierarchical normal (eight-schools pattern,
+  mcmc/eight_schools_hmc.py:41-58): state [mu, log tau, z_1..z_J]."""
+
+  def __init__(self, y, sigma, mu_scale=5.0, tau_scale=5.0):
+    y_t = _util.as_tensor(y, torch.float32).reshape(-1)
+    s_t = _util.as_tensor(sigma, torch.float32).reshape(-1)
+    if y_t.shape != s_t.shape:
+      raise ValueError('y and sigma must have one entry per group')
+    self.groups = y_t.shape[0]
+    ctx = _native.Context.current()
+    h = ctypes.c_void_p()
+    _native.check(_native.lib().gbm_target_hierarchical_normal(
+        ctx.handle, _native.ptr(y_t), _native.ptr(s_t), self.groups, float(mu_scale),
+        float(tau_scale), ctypes.byref(h)), 'gbm_target_hierarchical_normal')
+    self._handle = h
+    self._ctx = ctx
+
+
 def resolve(target_log_prob_fn):
   """Return the engine target behind ``target_log_prob_fn`` or raise."""
   t = target_log_prob_fn
