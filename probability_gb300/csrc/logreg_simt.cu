@@ -22,6 +22,7 @@
 #include <memory>
 
 #include "engine.h"
+#include "split_reduce.cuh"
 
 namespace gbm {
 
@@ -241,11 +242,8 @@ class LogregSimt final : public Target {
           x_.as<float>(), ldx_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart); break;
     }
     GBM_CUDA(cudaGetLastError());
-    const int warps_per_block = 8;
-    logreg_reduce_kernel<<<(cap + warps_per_block - 1) / warps_per_block, 32 * warps_per_block, 0,
-                           s>>>(lpart, gpart, q, ldq, n_dev, grid_, N, D, inv_var_, log_norm_,
-                                logp, grad, ldg);
-    GBM_CUDA(cudaGetLastError());
+    launch_split_reduce(lpart, gpart, q, ldq, n_dev, cap, kCT, kNT, grid_, N, D, inv_var_,
+                        log_norm_, logp, grad, ldg, s);
   }
 
   int launches_per_eval() const override { return 2; }

@@ -38,6 +38,7 @@
 #include <string>
 
 #include "engine.h"
+#include "split_reduce.cuh"
 #include "tc_ptx.cuh"
 
 namespace gbm {
@@ -439,45 +440,6 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
   }
 }
 
-__global__ void tc_reduce_kernel(const double* __restrict__ lpart, const float* __restrict__ gpart,
-                                 const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev,
-                                 int ct, int grid, int N, int D, float inv_var, double log_norm,
-                                 double* __restrict__ logp, float* __restrict__ grad, int ldg) {
-  const int n = *n_dev;
-  const int S = tc_splits(n, ct, grid, (N + kRows - 1) / kRows);
-  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  const int lane = threadIdx.x & 31;
-  if (warp >= n) return;
-  // Each lane owns features lane + 32k (k < 8, D <= 256): all of them are
-  // loaded for one split before the next, so a warp keeps up to 256
-  // independent loads in flight; splits are summed in fixed order.
-  const float* q = Q + (size_t)warp * ldq;
-  const size_t sstride = (size_t)n * D;
-  const float* p = gpart + (size_t)warp * D;
-  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  double lp = 0.0;
-  for (int s = 0; s < S; ++s) {
-#pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int d = lane + 32 * k;
-      if (d < D) acc[k] += p[(size_t)s * sstride + d];
-    }
-    if (lane == 0) lp += lpart[(size_t)s * n + warp];
-  }
-  double prior = 0.0;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int d = lane + 32 * k;
-    if (d < D) {
-      const float qd = q[d];
-      grad[(size_t)warp * ldg + d] = acc[k] - qd * inv_var;
-      prior += (double)qd * (double)qd;
-    }
-  }
-  prior = warp_sum(prior);
-  if (lane == 0) logp[warp] = lp - 0.5 * (double)inv_var * prior + (double)D * log_norm;
-}
-
 // FP32 X -> X_hi = bf16(X) and (optionally) X_lo = bf16(X - X_hi), zero-padded
 // to Dp features.
 __global__ void to_bf16_padded(const float* __restrict__ X, int64_t N, int D, int Dp,
@@ -588,9 +550,8 @@ class LogregTc final : public Target {
     else GBM_TC_LAUNCH(4, 64, 8, false);
 #undef GBM_TC_LAUNCH
     GBM_CUDA(cudaGetLastError());
-    tc_reduce_kernel<<<(cap + 7) / 8, 256, 0, s>>>(lpart, gpart, q, ldq, n_dev, ct_, grid_, N, D,
-                                                   inv_var_, log_norm_, logp, grad, ldg);
-    GBM_CUDA(cudaGetLastError());
+    launch_split_reduce(lpart, gpart, q, ldq, n_dev, cap, ct_, kRows, grid_, N, D, inv_var_,
+                        log_norm_, logp, grad, ldg, s);
   }
 
   int launches_per_eval() const override { return 2; }
