@@ -237,6 +237,91 @@ GBM_API int gbm_hmc_sample_chain(gbm_hmc* kernel, int64_t chains, float* state,
                                  double* trace_target_log_prob, double* trace_log_accept_ratio,
                                  uint8_t* trace_is_accepted, float* trace_step_size);
 
+/* ---- Job server: many independent posteriors at once ------------------- */
+
+/* There is no counterpart in the reference (it runs one sample_chain per
+ * Python call).  A server owns `workers` host threads, each with its own
+ * device stream.  Jobs -- one target family + DA(NUTS) sample_chain run --
+ * are admitted first-in first-out while their estimated device memory fits
+ * `memory_budget_bytes`; admitted jobs run concurrently on the workers'
+ * streams with all chain and adaptation state resident on the device, and
+ * their buffers come from the stream-ordered allocator so job set-up and
+ * tear-down never synchronize the device.  Kernels are deterministic, so a
+ * job's results do not depend on what else runs beside it. */
+#define GBM_FAMILY_LOGISTIC_REGRESSION 0
+#define GBM_FAMILY_MVN 1
+#define GBM_FAMILY_HIERARCHICAL_NORMAL 2
+
+#define GBM_JOB_QUEUED 0
+#define GBM_JOB_RUNNING 1
+#define GBM_JOB_DONE 2
+#define GBM_JOB_FAILED 3
+
+typedef struct gbm_server gbm_server;
+
+/* One posterior-sampling job.  Input pointers are device pointers that must
+ * stay valid until the job is DONE or FAILED; output pointers may be NULL. */
+typedef struct gbm_job_spec {
+  int32_t family;                 /* GBM_FAMILY_* */
+  /* logistic regression: x [rows][features] (x_dtype), y [rows] */
+  const void* x;
+  int32_t x_dtype;
+  int32_t precision;              /* GBM_PRECISION_* */
+  int64_t rows;
+  int64_t features;
+  const float* y;
+  float prior_scale;
+  /* multivariate normal: loc [dim], scale_tril_inv [dim][dim] */
+  const float* loc;
+  const float* scale_tril_inv;
+  double log_normalizer;
+  /* hierarchical normal: group_y, group_sigma [groups] */
+  const float* group_y;
+  const float* group_sigma;
+  int64_t groups;
+  float mu_scale;
+  float tau_scale;
+  /* sampler: DualAveragingStepSizeAdaptation(NoUTurnSampler) */
+  int64_t dim;                    /* must match the family's dimension */
+  int64_t chains;
+  const float* init_state;        /* [chains][dim] */
+  float step_size;                /* initial step size */
+  int32_t max_tree_depth;
+  int32_t num_adaptation_steps;   /* <= 0: fixed step size */
+  double target_accept_prob;
+  int64_t num_results;
+  int64_t num_burnin_steps;
+  uint32_t seed[2];
+  /* outputs (device) */
+  float* trace_state;             /* [num_results][chains][dim] */
+  double* trace_log_accept_ratio; /* [num_results][chains] */
+  int32_t* trace_leapfrogs_taken; /* [num_results][chains] */
+  float* final_state;             /* [chains][dim] */
+  float* final_step_size;         /* [1] */
+} gbm_job_spec;
+
+typedef struct gbm_job_info {
+  int32_t status;                 /* GBM_JOB_* */
+  int32_t error_code;             /* GBM_* status of a failed job */
+  double submit_s, start_s, end_s;  /* server clock (s since creation) */
+  int64_t device_bytes;           /* admission estimate */
+} gbm_job_info;
+
+GBM_API int gbm_server_create(int device, int32_t workers, int64_t memory_budget_bytes,
+                              gbm_server** out);
+/* Waits for running jobs to finish and drops queued ones. */
+GBM_API int gbm_server_destroy(gbm_server* server);
+GBM_API int gbm_server_submit(gbm_server* server, const gbm_job_spec* spec, int64_t* job_id);
+GBM_API int gbm_server_query(gbm_server* server, int64_t job_id, gbm_job_info* info);
+/* Blocks until the job is DONE or FAILED or `timeout_s` passes
+ * (GBM_ETIMEDOUT). */
+GBM_API int gbm_server_wait(gbm_server* server, int64_t job_id, double timeout_s,
+                            gbm_job_info* info);
+/* Forget a finished job's record. */
+GBM_API int gbm_server_release(gbm_server* server, int64_t job_id);
+/* Seconds since the server was created (the clock of gbm_job_info). */
+GBM_API double gbm_server_now(gbm_server* server);
+
 /* ---- DualAveragingStepSizeAdaptation ----------------------------------- */
 
 /* One dual-averaging update after an inner one_step

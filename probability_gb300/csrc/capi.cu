@@ -17,6 +17,29 @@ static thread_local std::string g_last_error;
 
 void set_error(const std::string& msg) { g_last_error = msg; }
 
+void context_init(gbm_context* ctx, int device, cudaStream_t stream, bool owns_stream) {
+  ctx->device = device;
+  ctx->stream = stream;   // NULL: the default stream
+  ctx->owns_stream = owns_stream;
+  GBM_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
+  ctx->host_flag_slots = 16;
+  GBM_CUDA(cudaMallocHost(&ctx->host_flags, sizeof(int) * ctx->host_flag_slots));
+  void* errp = nullptr;
+  GBM_CUDA(cudaHostAlloc(&errp, 64, cudaHostAllocMapped));
+  ctx->err_host = static_cast<volatile int*>(errp);
+  *ctx->err_host = 0;
+  GBM_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->err_dev), errp, 0));
+}
+
+void context_free(gbm_context* ctx) {
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->host_flags) cudaFreeHost(ctx->host_flags);
+  if (ctx->err_host) cudaFreeHost(const_cast<int*>(ctx->err_host));
+  if (ctx->owns_stream) cudaStreamDestroy(ctx->stream);
+  ctx->host_flags = nullptr;
+  ctx->err_host = nullptr;
+}
+
 std::unique_ptr<Target> make_logreg_tc(gbm_context* ctx, const void* X, int x_dtype, int64_t n,
                                        int64_t d, const float* y, float prior_scale);
 
@@ -89,17 +112,7 @@ int gbm_context_create(int device, void* stream, gbm_context** out) {
     if (device < 0 || device >= n) return invalid("gbm_context_create: bad device index");
     DeviceGuard g(device);
     auto* ctx = new gbm_context();
-    ctx->device = device;
-    ctx->stream = static_cast<cudaStream_t>(stream);   // NULL: the default stream
-    ctx->owns_stream = false;
-    GBM_CUDA(cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device));
-    ctx->host_flag_slots = 16;
-    GBM_CUDA(cudaMallocHost(&ctx->host_flags, sizeof(int) * ctx->host_flag_slots));
-    void* errp = nullptr;
-    GBM_CUDA(cudaHostAlloc(&errp, 64, cudaHostAllocMapped));
-    ctx->err_host = static_cast<volatile int*>(errp);
-    *ctx->err_host = 0;
-    GBM_CUDA(cudaHostGetDevicePointer(reinterpret_cast<void**>(&ctx->err_dev), errp, 0));
+    gbm::context_init(ctx, device, static_cast<cudaStream_t>(stream), false);
     *out = ctx;
     return GBM_OK;
   });

@@ -27,20 +27,36 @@ struct gbm_context {
 namespace gbm {
 
 // Device memory owned by a handle; freed on destruction.
+// Stream for stream-ordered allocation on this host thread (nullptr: plain
+// cudaMalloc/cudaFree).  Job-server workers set it to their private stream so
+// that creating and freeing a job's buffers never synchronizes the device.
+cudaStream_t& alloc_stream();
+
 struct DeviceBuffer {
   void* ptr = nullptr;
   size_t bytes = 0;
+  cudaStream_t stream = nullptr;   // allocation stream (stream-ordered if set)
   DeviceBuffer() = default;
   DeviceBuffer(const DeviceBuffer&) = delete;
   DeviceBuffer& operator=(const DeviceBuffer&) = delete;
-  ~DeviceBuffer() { if (ptr) cudaFree(ptr); }
-  void reserve(size_t b) {
-    if (b <= bytes) return;
-    if (ptr) cudaFree(ptr);
+  ~DeviceBuffer() { release(); }
+  void release() {
+    if (ptr) {
+      if (stream) cudaFreeAsync(ptr, stream); else cudaFree(ptr);
+    }
     ptr = nullptr;
     bytes = 0;
+  }
+  void reserve(size_t b) {
+    if (b <= bytes) return;
+    release();
     if (b == 0) return;
-    GBM_CUDA(cudaMalloc(&ptr, b));
+    stream = alloc_stream();
+    if (stream) {
+      GBM_CUDA(cudaMallocAsync(&ptr, b, stream));
+    } else {
+      GBM_CUDA(cudaMalloc(&ptr, b));
+    }
     bytes = b;
   }
   template <class T> T* as() const { return static_cast<T*>(ptr); }
@@ -63,6 +79,11 @@ struct Target {
   // Kernels one eval() launches (for launch accounting).
   virtual int launches_per_eval() const = 0;
 };
+
+// Fill / release a context (pinned host words, mapped error word).
+void context_init(gbm_context* ctx, int device, cudaStream_t stream, bool owns_stream);
+void context_free(gbm_context* ctx);
+void set_error(const std::string& msg);
 
 // Raise (and clear) an error a kernel stored in the context's error word.
 inline void check_device_error(gbm_context* ctx) {

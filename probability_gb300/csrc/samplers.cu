@@ -77,6 +77,11 @@ __global__ void build_active_kernel(const uint8_t* __restrict__ flags, uint8_t b
   if (tid == 0) *count = base_s;
 }
 
+cudaStream_t& alloc_stream() {
+  static thread_local cudaStream_t s = nullptr;
+  return s;
+}
+
 __global__ void set_count_kernel(int* count, int n) { *count = n; }
 
 void set_count(int* count, int n, cudaStream_t s) {
@@ -561,7 +566,7 @@ void nuts_setup(gbm_nuts* k) {
   w.act_count = iv + 4 * C; w.any_cont = iv + 4 * C + 1;
   w.flags = reinterpret_cast<uint8_t*>(base + off_b);
   w.eps = reinterpret_cast<float*>(base + off_e);
-  GBM_CUDA(cudaMemset(base, 0, bytes));
+  GBM_CUDA(cudaMemsetAsync(base, 0, bytes, k->ctx->stream));
   k->target_ws.reserve(k->target->impl->workspace_bytes(C));
   for (auto& ev : k->poll_events) GBM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
 }
