@@ -243,7 +243,7 @@ class LogregSimt final : public Target {
     }
     GBM_CUDA(cudaGetLastError());
     launch_split_reduce(lpart, gpart, q, ldq, n_dev, cap, kCT, kNT, grid_, N, D, inv_var_,
-                        log_norm_, logp, grad, ldg, s);
+                        log_norm_, nullptr, logp, grad, ldg, s);
   }
 
   int launches_per_eval() const override { return 2; }

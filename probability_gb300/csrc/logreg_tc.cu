@@ -48,8 +48,9 @@ constexpr int kRows = 128;                         // rows of X per tile
 // Threads of a CTA with EPI epilogue warps (plus the TMA and MMA warps).
 __host__ __device__ constexpr int tc_threads(int epi) { return 32 * (2 + epi); }
 constexpr uint64_t kWaitLimitNs = 2000000000ull;   // 2 s bound on every device wait
-constexpr float kLog2e = 1.4426950408889634f;
+constexpr float kNeg2Log2e = -2.8853900817779268f;  // -2 log2(e)
 constexpr float kLn2 = 0.6931471805599453f;
+constexpr int kFlushTiles = 32;   // row tiles between folds of the running products
 
 enum TcError : int {
   kTcOk = 0,
@@ -95,6 +96,15 @@ struct Bars {
 __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   __nv_bfloat162 v = __floats2bfloat162_rn(a, b);
   return *reinterpret_cast<uint32_t*>(&v);
+}
+
+// R = y - sigmoid(z) for two elements, from h = z / 2: sigmoid(z) = 1/2 +
+// tanh(h) / 2, so R = (y - 1/2) - tanh(h) / 2, rounded to nearest BF16 (the
+// contraction's operand type; round-to-nearest keeps the rounding unbiased,
+// which matters for the intercept column, whose gradient sums R over all
+// rows).
+__device__ __forceinline__ uint32_t residual_bf16x2(float h0, float h1, float ym) {
+  return pack_bf16x2(fmaf(-0.5f, tc::tanh_approx(h0), ym), fmaf(-0.5f, tc::tanh_approx(h1), ym));
 }
 
 __device__ __forceinline__ void named_barrier(int id, int nthreads) {
@@ -170,7 +180,9 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
   }
   if (warp == 1) tc::tmem_alloc(tmem_slot, L::kTmemCols);
 
-  // Chain states -> BF16 hi/lo, K-major 128-byte-swizzled [KB][CT][128 B].
+  // Chain states / 2 -> BF16 hi/lo, K-major 128-byte-swizzled [KB][CT][128 B].
+  // The factor 1/2 (exact) makes the accumulator hold h = z / 2, the argument
+  // the epilogue needs for both tanh and exp.
   for (int i = tid; i < CT * KB * 8; i += kThreads) {
     const int c = i / (KB * 8), chunk = i % (KB * 8);
     const int d0 = chunk * 8;
@@ -178,7 +190,7 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
 #pragma unroll
     for (int e = 0; e < 8; ++e) {
       const int d = d0 + e;
-      v[e] = (c0 + c < n && d < D) ? Q[(size_t)(c0 + c) * ldq + d] : 0.f;
+      v[e] = (c0 + c < n && d < D) ? 0.5f * Q[(size_t)(c0 + c) * ldq + d] : 0.f;
     }
     uint32_t hi[4], lo[4];
 #pragma unroll
@@ -245,6 +257,7 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
       const uint32_t xs_a = tc::smem_u32(Xs), bhi_a = tc::smem_u32(Bhi);
       const uint32_t blo_a = tc::smem_u32(Blo), rs_a = tc::smem_u32(Rs);
       const uint32_t tg = tmem + 2 * CT;
+      const int ksteps = (D + 15) >> 4;   // K-steps of 16 features holding data
       bool ok = true;
       auto gemm1 = [&](int it) -> bool {
         const int s = it & 1, b = it & 1;
@@ -262,6 +275,7 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
         for (int kb = 0; kb < KB; ++kb) {
 #pragma unroll
           for (int k = 0; k < 4; ++k) {
+            if (kb * 4 + k >= ksteps) break;   // all-zero padding features
             const uint64_t a = tc::smem_desc_sw128(xa + kb * 16384 + k * 32, 16, 1024);
             const uint64_t bh = tc::smem_desc_sw128(bhi_a + kb * (CT * 128) + k * 32, 16, 1024);
             const uint64_t bl = tc::smem_desc_sw128(blo_a + kb * (CT * 128) + k * 32, 16, 1024);
@@ -320,9 +334,19 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
     const int half = (warp - 2) >> 2;             // chains [half*kCW, +kCW)
     const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
     const int r = quarter * 32 + lane;            // row of the tile this thread owns
-    float lp_acc[kCW];
+    // Per chain: softplus(z) = max(z, 0) + ln(1 + e^-|z|) and max(z, 0) =
+    // z/2 + |h|, so sum_r log Bernoulli(y_r | z_r) = sum_r (y_r - 1/2) z_r
+    // - sum_r |h_r| - sum_r ln(1 + e^-|z_r|).  The first sum is linear in the
+    // state and is added exactly by the reduction; here sacc accumulates
+    // |h| and pacc the running product of (1 + e^-|z|) (one FMA per element;
+    // its logarithm is folded into sacc every kFlushTiles tiles, before the
+    // product could exceed 2^kFlushTiles).
+    float pacc[kCW], sacc[kCW];
 #pragma unroll
-    for (int c = 0; c < kCW; ++c) lp_acc[c] = 0.f;
+    for (int c = 0; c < kCW; ++c) {
+      pacc[c] = 1.f;
+      sacc[c] = 0.f;
+    }
     bool ok = true;
     // y of this thread's row, prefetched one tile ahead.
     float y_next = 0.f;
@@ -341,45 +365,32 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
       tc::tc_fence_after();
       const int row = (rt_begin + it) * kRows + r;
       const bool valid = row < N;
-      const float yv = valid ? y_next : 0.f;
+      const float ym = (valid ? y_next : 0.f) - 0.5f;
       if (it + 1 < T && row + kRows < N) y_next = y[row + kRows];
       const uint32_t tz = tmem + b * CT + half * kCW;
       unsigned char* Rb = Rs + b * L::kRBuf;
-      float zall[kCW];
+      // Groups of 8 chains: one 8-column TMEM load, one 16-byte R store (few
+      // live registers beside the per-chain accumulators).
 #pragma unroll
-      for (int q = 0; q < kCW / 32; ++q) tc::tmem_ld32(tz + lane_base + q * 32, zall + q * 32);
-      tc::tmem_ld_wait();
-#pragma unroll
-      for (int ch = 0; ch < kCW / 16; ++ch) {
-        const float* z = zall + ch * 16;
-        float rv[16];
-        // log Bernoulli(y | z) = y z - softplus(z), softplus(z) = max(z, 0) +
-        // ln2 * log2(1 + 2^(-|z| log2 e)).  The sigmoid only feeds the BF16
-        // gradient contraction, so the tanh form 0.5 + 0.5 tanh(z / 2) (one
-        // special-function op) is accurate enough for it.
+      for (int g8 = 0; g8 < kCW / 8; ++g8) {
+        float h[8];
+        tc::tmem_ld8(tz + lane_base + g8 * 8, h);
+        tc::tmem_ld_wait();
+        uint32_t rp[4] = {0u, 0u, 0u, 0u};                   // rows past N: R = 0
         if (valid) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
-            const float zz = z[j];
-            const float t = tc::ex2_approx(-fabsf(zz) * kLog2e);
-            const float lg = tc::lg2_approx(1.f + t);
-            lp_acc[ch * 16 + j] =
-                fmaf(-kLn2, lg, lp_acc[ch * 16 + j] + fmaf(yv, zz, -fmaxf(zz, 0.f)));
-            rv[j] = yv - fmaf(0.5f, tc::tanh_approx(0.5f * zz), 0.5f);
+          for (int j = 0; j < 8; ++j) {
+            const float a = fabsf(h[j]);
+            const float t = tc::ex2_approx(a * kNeg2Log2e);     // e^-|z|
+            pacc[g8 * 8 + j] = fmaf(pacc[g8 * 8 + j], t, pacc[g8 * 8 + j]);
+            sacc[g8 * 8 + j] += a;
           }
-        } else {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) rv[j] = 0.f;   // rows past N
+          for (int j = 0; j < 4; ++j) rp[j] = residual_bf16x2(h[2 * j], h[2 * j + 1], ym);
         }
-        const int c = half * kCW + ch * 16;
-        const uint32_t off0 = (c >> 6) * 16384 + tc::sw128_offset(r, c & 63);
-        const uint32_t off1 = ((c + 8) >> 6) * 16384 + tc::sw128_offset(r, (c + 8) & 63);
-        *reinterpret_cast<uint4*>(Rb + off0) =
-            make_uint4(pack_bf16x2(rv[0], rv[1]), pack_bf16x2(rv[2], rv[3]),
-                       pack_bf16x2(rv[4], rv[5]), pack_bf16x2(rv[6], rv[7]));
-        *reinterpret_cast<uint4*>(Rb + off1) =
-            make_uint4(pack_bf16x2(rv[8], rv[9]), pack_bf16x2(rv[10], rv[11]),
-                       pack_bf16x2(rv[12], rv[13]), pack_bf16x2(rv[14], rv[15]));
+        const int c = half * kCW + g8 * 8;
+        *reinterpret_cast<uint4*>(Rb + (c >> 6) * 16384 + tc::sw128_offset(r, c & 63)) =
+            make_uint4(rp[0], rp[1], rp[2], rp[3]);
       }
       tc::tc_fence_before();
       tc::fence_proxy_async_smem();
@@ -387,6 +398,13 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
       if (lane == 0) {
         tc::mbar_arrive(&bars->z_empty[b]);
         tc::mbar_arrive(&bars->r_full[b]);
+      }
+      if ((it % kFlushTiles) == kFlushTiles - 1) {
+#pragma unroll
+        for (int c = 0; c < kCW; ++c) {
+          sacc[c] = fmaf(kLn2, tc::lg2_approx(pacc[c]), sacc[c]);
+          pacc[c] = 1.f;
+        }
       }
     }
     if (ok && T > 0) ok = wait_or_abort(&bars->g_done, 0, abort_flag);
@@ -413,12 +431,12 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
           }
         }
       }
-      // Log-likelihood partials: sum over the 128 rows per chain.
+      // Nonlinear log-likelihood partials: minus the sum over the 128 rows per
+      // chain (FP32 shuffles: the FP64 pipe of this GPU is far too narrow for
+      // a per-chain warp reduction; only the final 4-way sum is FP64).
 #pragma unroll
-      // (FP32 shuffles: the FP64 pipe of this GPU is far too narrow for a
-      // per-chain warp reduction; only the final 4-way sum is FP64.)
       for (int c = 0; c < kCW; ++c) {
-        float v = lp_acc[c];
+        float v = -fmaf(kLn2, tc::lg2_approx(pacc[c]), sacc[c]);
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) red[quarter * CT + half * kCW + c] = (double)v;
@@ -461,6 +479,36 @@ __global__ void bf16_pad(const __nv_bfloat16* __restrict__ X, int64_t N, int D, 
   const int64_t r = i / Dp;
   const int d = (int)(i % Dp);
   out[i] = d < D ? X[r * D + d] : __float2bfloat16_rn(0.f);
+}
+
+// lin[d] = sum_r (y_r - 1/2) X[r][d] in float64, in a fixed order (so every
+// target built from the same data gets the same bits): block b sums rows
+// [b * chunk, (b + 1) * chunk) into part[b][d], then lin_sum_kernel adds the
+// blocks in index order.
+__device__ __forceinline__ double as_double(float v) { return (double)v; }
+__device__ __forceinline__ double as_double(__nv_bfloat16 v) {
+  return (double)__bfloat162float(v);
+}
+
+template <class T>
+__global__ void lin_partial_kernel(const T* __restrict__ X, const float* __restrict__ y,
+                                   int64_t N, int D, int64_t chunk, double* __restrict__ part) {
+  const int64_t r0 = (int64_t)blockIdx.x * chunk;
+  const int64_t r1 = r0 + chunk < N ? r0 + chunk : N;
+  for (int d = threadIdx.x; d < D; d += blockDim.x) {
+    double acc = 0.0;
+    for (int64_t r = r0; r < r1; ++r) acc += ((double)y[r] - 0.5) * as_double(X[r * D + d]);
+    part[(size_t)blockIdx.x * D + d] = acc;
+  }
+}
+
+__global__ void lin_sum_kernel(const double* __restrict__ part, int nb, int D,
+                               double* __restrict__ lin) {
+  const int d = blockIdx.x * blockDim.x + threadIdx.x;
+  if (d >= D) return;
+  double acc = 0.0;
+  for (int b = 0; b < nb; ++b) acc += part[(size_t)b * D + d];
+  lin[d] = acc;
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
@@ -510,6 +558,25 @@ class LogregTc final : public Target {
     GBM_CUDA(cudaGetLastError());
     GBM_CUDA(cudaMemcpyAsync(y_.ptr, y, sizeof(float) * N_, cudaMemcpyDeviceToDevice,
                              ctx->stream));
+    {
+      const int nb = 2 * ctx->num_sms;
+      const int64_t chunk = (N_ + nb - 1) / nb;
+      DeviceBuffer part;
+      part.reserve(sizeof(double) * (size_t)nb * D_);
+      lin_.reserve(sizeof(double) * (size_t)D_);
+      if (x_dtype == 0)
+        lin_partial_kernel<<<nb, 256, 0, ctx->stream>>>(static_cast<const float*>(X), y, N_,
+                                                        (int)D_, chunk, part.as<double>());
+      else
+        lin_partial_kernel<<<nb, 256, 0, ctx->stream>>>(static_cast<const __nv_bfloat16*>(X),
+                                                        y, N_, (int)D_, chunk,
+                                                        part.as<double>());
+      lin_sum_kernel<<<(unsigned)((D_ + 127) / 128), 128, 0, ctx->stream>>>(
+          part.as<double>(), nb, (int)D_, lin_.as<double>());
+      GBM_CUDA(cudaGetLastError());
+      // `part` is freed on scope exit: finish the sum first.
+      GBM_CUDA(cudaStreamSynchronize(ctx->stream));
+    }
     inv_var_ = 1.f / (prior_scale * prior_scale);
     log_norm_ = -log((double)prior_scale) - 0.5 * log(2.0 * M_PI);
     grid_ = ctx->num_sms;
@@ -551,7 +618,7 @@ class LogregTc final : public Target {
 #undef GBM_TC_LAUNCH
     GBM_CUDA(cudaGetLastError());
     launch_split_reduce(lpart, gpart, q, ldq, n_dev, cap, ct_, kRows, grid_, N, D, inv_var_,
-                        log_norm_, logp, grad, ldg, s);
+                        log_norm_, lin_.as<double>(), logp, grad, ldg, s);
   }
 
   int launches_per_eval() const override { return 2; }
@@ -581,6 +648,7 @@ class LogregTc final : public Target {
   }
 
   DeviceBuffer xb_, xl_, y_;
+  DeviceBuffer lin_;   // X^T (y - 1/2), float64 [D]
   bool xlo_ = false;
   CUtensorMap xlomap_;
   int* err_dev_ = nullptr;

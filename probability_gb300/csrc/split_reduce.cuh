@@ -8,6 +8,11 @@
 // owns features lane + 32k, D <= 256), then the W partial sums are combined
 // in warp order.  The order depends only on S, so results are reproducible;
 // with many splits (few chains) all W warps keep loads in flight.
+//
+// `lin` (optional, float64 [D]) adds lin . q_c to each chain's log-density:
+// the tensor-core kernel leaves the linear part sum_r (y_r - 1/2) z_rc of the
+// Bernoulli log-likelihood to this pass as (X^T (y - 1/2)) . q_c, exact in
+// float64.
 #pragma once
 #include <cuda_runtime.h>
 
@@ -32,7 +37,8 @@ __global__ void __launch_bounds__(32 * kReduceWarps)
 split_reduce_kernel(const double* __restrict__ lpart, const float* __restrict__ gpart,
                     const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev, int ct,
                     int nt, int grid, int N, int D, float inv_var, double log_norm,
-                    double* __restrict__ logp, float* __restrict__ grad, int ldg) {
+                    const double* __restrict__ lin, double* __restrict__ logp,
+                    float* __restrict__ grad, int ldg) {
   const int n = *n_dev;
   const int c = blockIdx.x;
   if (c >= n) return;
@@ -57,13 +63,15 @@ split_reduce_kernel(const double* __restrict__ lpart, const float* __restrict__ 
   for (int k = 0; k < 8; ++k) gsum[warp][lane + 32 * k] = acc[k];
   if (lane == 0) lsum[warp] = lp;
   if (warp == 0) {
-    double pr = 0.0;
+    double pr = 0.0, li = 0.0;
     for (int d = lane; d < D; d += 32) {
       const double qd = (double)Q[(size_t)c * ldq + d];
       pr += qd * qd;
+      if (lin) li += lin[d] * qd;
     }
     pr = warp_sum(pr);
-    if (lane == 0) prior_s = pr;
+    li = warp_sum(li);
+    if (lane == 0) prior_s = li - 0.5 * (double)inv_var * pr;
   }
   __syncthreads();
   for (int d = threadIdx.x; d < D; d += 32 * kReduceWarps) {
@@ -76,16 +84,17 @@ split_reduce_kernel(const double* __restrict__ lpart, const float* __restrict__ 
     double t = 0.0;
 #pragma unroll
     for (int w = 0; w < kReduceWarps; ++w) t += lsum[w];
-    logp[c] = t - 0.5 * (double)inv_var * prior_s + (double)D * log_norm;
+    logp[c] = t + prior_s + (double)D * log_norm;
   }
 }
 
 void launch_split_reduce(const double* lpart, const float* gpart, const float* Q, int ldq,
                          const int* n_dev, int cap, int ct, int nt, int grid, int N, int D,
-                         float inv_var, double log_norm, double* logp, float* grad, int ldg,
-                         cudaStream_t s) {
+                         float inv_var, double log_norm, const double* lin, double* logp,
+                         float* grad, int ldg, cudaStream_t s) {
   split_reduce_kernel<<<cap, 32 * kReduceWarps, 0, s>>>(lpart, gpart, Q, ldq, n_dev, ct, nt, grid,
-                                                       N, D, inv_var, log_norm, logp, grad, ldg);
+                                                       N, D, inv_var, log_norm, lin, logp, grad,
+                                                       ldg);
   GBM_CUDA(cudaGetLastError());
 }
 
