@@ -50,7 +50,6 @@ __host__ __device__ constexpr int tc_threads(int epi) { return 32 * (2 + epi); }
 constexpr uint64_t kWaitLimitNs = 2000000000ull;   // 2 s bound on every device wait
 constexpr float kNeg2Log2e = -2.8853900817779268f;  // -2 log2(e)
 constexpr float kLn2 = 0.6931471805599453f;
-constexpr int kFlushTiles = 32;   // row tiles between folds of the running products
 
 enum TcError : int {
   kTcOk = 0,
@@ -67,29 +66,35 @@ __host__ __device__ inline int tc_splits(int n, int ct, int grid, int row_tiles)
   return s > row_tiles ? row_tiles : s;
 }
 
+// Shared memory.  With up to 128 features, X_hi has three stages so that the
+// TMA refill of a stage (which can start only once GEMM2 has read it) runs a
+// full tile ahead of the GEMM1 that needs it; R is then single-buffered (the
+// epilogue waits for GEMM2 to release it only just before its first store).
 template <int KB, int CT, bool XLO>
 struct TcLayout {
+  static constexpr int kStages = KB == 2 ? 3 : 2;      // X_hi stages
+  static constexpr int kRBufs = KB == 2 ? 1 : 2;       // R buffers
   static constexpr int kXStage = KB * 16384;           // [KB][128 rows][128 B]
   static constexpr int kBBytes = KB * CT * 128;        // [KB][CT rows][128 B]
   static constexpr int kRBuf = (CT / 64) * 16384;      // [CT/64][128 rows][128 B]
-  static constexpr int kX = 0;                         // 2 stages
-  static constexpr int kBhi = kX + 2 * kXStage;
+  static constexpr int kX = 0;
+  static constexpr int kBhi = kX + kStages * kXStage;
   static constexpr int kBlo = kBhi + kBBytes;
-  static constexpr int kR = kBlo + kBBytes;            // 2 buffers
-  static constexpr int kXlo = kR + 2 * kRBuf;          // X residual, 1 stage (XLO only)
+  static constexpr int kR = kBlo + kBBytes;
+  static constexpr int kXlo = kR + kRBufs * kRBuf;     // X residual, 1 stage (XLO only)
   static constexpr int kCtl = kXlo + (XLO ? kXStage : 0);  // barriers + tmem slot + abort
   // After the last MMA the R buffers are reused for the [4 quarters][CT]
   // double log-likelihood reduction.
   static constexpr int kRed = kR;
   static constexpr int kBytes = kCtl + 256;
-  static_assert(4 * CT * 8 <= 2 * kRBuf, "reduction scratch must fit the R buffers");
+  static_assert(4 * CT * 8 <= kRBufs * kRBuf, "reduction scratch must fit the R buffers");
   static constexpr int kMTiles = KB / 2;               // 128-feature tiles of G
   static constexpr uint32_t kTmemCols = (2 * CT + kMTiles * CT) <= 256 ? 256 : 512;
   static_assert(kBytes + 1024 <= 232448, "shared memory over the sm_103a limit");
 };
 
 struct Bars {
-  uint64_t x_full[2], x_empty[2], z_full[2], z_empty[2], r_full[2], r_empty[2], g_done, drain;
+  uint64_t x_full[3], x_empty[3], z_full[2], z_empty[2], r_full[2], r_empty[2], g_done, drain;
   uint64_t xlo_full, xlo_empty;
 };
 
@@ -162,9 +167,11 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
 
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) {
-    for (int i = 0; i < 2; ++i) {
+    for (int i = 0; i < 3; ++i) {
       tc::mbar_init(&bars->x_full[i], 1);
       tc::mbar_init(&bars->x_empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
       tc::mbar_init(&bars->z_full[i], 1);
       tc::mbar_init(&bars->z_empty[i], EPI);
       tc::mbar_init(&bars->r_full[i], EPI);
@@ -215,8 +222,8 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
     if (lane == 0) {
       int it = 0;
       for (; it < T; ++it) {
-        const int s = it & 1;
-        const uint32_t use = (uint32_t)(it >> 1);
+        const int s = it % L::kStages;
+        const uint32_t use = (uint32_t)(it / L::kStages);
         if (!wait_or_abort(&bars->x_empty[s], (use & 1) ^ 1, abort_flag)) {
           tc::record_error(err,kTcTimeoutTma);
           *abort_flag = 1;
@@ -243,8 +250,9 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
         }
       }
       // Drain: every issued load has landed before the CTA can exit.
-      for (int j = (it > 2 ? it - 2 : 0); j < it; ++j)
-        tc::mbar_wait(&bars->x_full[j & 1], (uint32_t)((j >> 1) & 1), kWaitLimitNs);
+      for (int j = (it > L::kStages ? it - L::kStages : 0); j < it; ++j)
+        tc::mbar_wait(&bars->x_full[j % L::kStages], (uint32_t)((j / L::kStages) & 1),
+                      kWaitLimitNs);
       if constexpr (XLO) {
         if (it > 0) tc::mbar_wait(&bars->xlo_full, (uint32_t)((it - 1) & 1), kWaitLimitNs);
       }
@@ -260,10 +268,11 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
       const int ksteps = (D + 15) >> 4;   // K-steps of 16 features holding data
       bool ok = true;
       auto gemm1 = [&](int it) -> bool {
-        const int s = it & 1, b = it & 1;
-        const uint32_t use = (uint32_t)(it >> 1);
-        if (!wait_or_abort(&bars->x_full[s], use & 1, abort_flag)) return false;
-        if (!wait_or_abort(&bars->z_empty[b], (use & 1) ^ 1, abort_flag)) return false;
+        const int s = it % L::kStages, b = it & 1;
+        if (!wait_or_abort(&bars->x_full[s], (uint32_t)(it / L::kStages) & 1, abort_flag))
+          return false;
+        if (!wait_or_abort(&bars->z_empty[b], ((uint32_t)(it >> 1) & 1) ^ 1, abort_flag))
+          return false;
         if constexpr (XLO) {
           if (!wait_or_abort(&bars->xlo_full, (uint32_t)(it & 1), abort_flag)) return false;
         }
@@ -297,15 +306,14 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
           ok = gemm1(it + 1);
           if (!ok) break;
         }
-        const int s = it & 1, b = it & 1;
-        const uint32_t use = (uint32_t)(it >> 1);
-        if (!wait_or_abort(&bars->r_full[b], use & 1, abort_flag)) {
+        const int s = it % L::kStages, rb = it % L::kRBufs;
+        if (!wait_or_abort(&bars->r_full[rb], (uint32_t)(it / L::kRBufs) & 1, abort_flag)) {
           ok = false;
           break;
         }
         tc::tc_fence_after();
         const uint32_t xa = xs_a + s * L::kXStage;
-        const uint32_t ra = rs_a + b * L::kRBuf;
+        const uint32_t ra = rs_a + rb * L::kRBuf;
 #pragma unroll
         for (int mt = 0; mt < L::kMTiles; ++mt) {
 #pragma unroll
@@ -316,7 +324,7 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
           }
         }
         tc::mma_commit(&bars->x_empty[s]);
-        tc::mma_commit(&bars->r_empty[b]);
+        tc::mma_commit(&bars->r_empty[rb]);
       }
       if (ok) {
         tc::mma_commit(&bars->g_done);
@@ -336,17 +344,13 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
     const int r = quarter * 32 + lane;            // row of the tile this thread owns
     // Per chain: softplus(z) = max(z, 0) + ln(1 + e^-|z|) and max(z, 0) =
     // z/2 + |h|, so sum_r log Bernoulli(y_r | z_r) = sum_r (y_r - 1/2) z_r
-    // - sum_r |h_r| - sum_r ln(1 + e^-|z_r|).  The first sum is linear in the
-    // state and is added exactly by the reduction; here sacc accumulates
-    // |h| and pacc the running product of (1 + e^-|z|) (one FMA per element;
-    // its logarithm is folded into sacc every kFlushTiles tiles, before the
-    // product could exceed 2^kFlushTiles).
-    float pacc[kCW], sacc[kCW];
+    // - sum_r (|h_r| + ln(1 + e^-|z_r|)).  The first sum is linear in the
+    // state and is added exactly by the reduction; sacc accumulates the
+    // second (one accumulator per chain leaves room for the whole row of Z
+    // in registers: one TMEM load and one wait per tile).
+    float sacc[kCW];
 #pragma unroll
-    for (int c = 0; c < kCW; ++c) {
-      pacc[c] = 1.f;
-      sacc[c] = 0.f;
-    }
+    for (int c = 0; c < kCW; ++c) sacc[c] = 0.f;
     bool ok = true;
     // y of this thread's row, prefetched one tile ahead.
     float y_next = 0.f;
@@ -355,10 +359,8 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
       if (T > 0 && row0 < N) y_next = y[row0];
     }
     for (int it = 0; it < T; ++it) {
-      const int b = it & 1;
-      const uint32_t use = (uint32_t)(it >> 1);
-      if (!wait_or_abort(&bars->z_full[b], use & 1, abort_flag) ||
-          !wait_or_abort(&bars->r_empty[b], (use & 1) ^ 1, abort_flag)) {
+      const int b = it & 1, rb = it % L::kRBufs;
+      if (!wait_or_abort(&bars->z_full[b], (uint32_t)(it >> 1) & 1, abort_flag)) {
         ok = false;
         break;
       }
@@ -368,43 +370,46 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
       const float ym = (valid ? y_next : 0.f) - 0.5f;
       if (it + 1 < T && row + kRows < N) y_next = y[row + kRows];
       const uint32_t tz = tmem + b * CT + half * kCW;
-      unsigned char* Rb = Rs + b * L::kRBuf;
-      // Groups of 8 chains: one 8-column TMEM load, one 16-byte R store (few
-      // live registers beside the per-chain accumulators).
+      unsigned char* Rb = Rs + rb * L::kRBuf;
+      float h[kCW];
+#pragma unroll
+      for (int q = 0; q < kCW / 32; ++q) tc::tmem_ld32(tz + lane_base + q * 32, h + q * 32);
+      tc::tmem_ld_wait();
+      bool r_free = false;
 #pragma unroll
       for (int g8 = 0; g8 < kCW / 8; ++g8) {
-        float h[8];
-        tc::tmem_ld8(tz + lane_base + g8 * 8, h);
-        tc::tmem_ld_wait();
         uint32_t rp[4] = {0u, 0u, 0u, 0u};                   // rows past N: R = 0
         if (valid) {
 #pragma unroll
           for (int j = 0; j < 8; ++j) {
-            const float a = fabsf(h[j]);
+            const float a = fabsf(h[g8 * 8 + j]);
             const float t = tc::ex2_approx(a * kNeg2Log2e);     // e^-|z|
-            pacc[g8 * 8 + j] = fmaf(pacc[g8 * 8 + j], t, pacc[g8 * 8 + j]);
-            sacc[g8 * 8 + j] += a;
+            sacc[g8 * 8 + j] += fmaf(kLn2, tc::lg2_approx(1.f + t), a);
           }
 #pragma unroll
-          for (int j = 0; j < 4; ++j) rp[j] = residual_bf16x2(h[2 * j], h[2 * j + 1], ym);
+          for (int j = 0; j < 4; ++j)
+            rp[j] = residual_bf16x2(h[g8 * 8 + 2 * j], h[g8 * 8 + 2 * j + 1], ym);
+        }
+        if (g8 == 0) {
+          // GEMM2 of the tile that last used this R buffer must be done.
+          r_free = wait_or_abort(&bars->r_empty[rb], ((uint32_t)(it / L::kRBufs) & 1) ^ 1,
+                                 abort_flag);
+          if (!r_free) break;
         }
         const int c = half * kCW + g8 * 8;
         *reinterpret_cast<uint4*>(Rb + (c >> 6) * 16384 + tc::sw128_offset(r, c & 63)) =
             make_uint4(rp[0], rp[1], rp[2], rp[3]);
+      }
+      if (!r_free) {
+        ok = false;
+        break;
       }
       tc::tc_fence_before();
       tc::fence_proxy_async_smem();
       __syncwarp();
       if (lane == 0) {
         tc::mbar_arrive(&bars->z_empty[b]);
-        tc::mbar_arrive(&bars->r_full[b]);
-      }
-      if ((it % kFlushTiles) == kFlushTiles - 1) {
-#pragma unroll
-        for (int c = 0; c < kCW; ++c) {
-          sacc[c] = fmaf(kLn2, tc::lg2_approx(pacc[c]), sacc[c]);
-          pacc[c] = 1.f;
-        }
+        tc::mbar_arrive(&bars->r_full[rb]);
       }
     }
     if (ok && T > 0) ok = wait_or_abort(&bars->g_done, 0, abort_flag);
@@ -436,7 +441,7 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
       // a per-chain warp reduction; only the final 4-way sum is FP64).
 #pragma unroll
       for (int c = 0; c < kCW; ++c) {
-        float v = -fmaf(kLn2, tc::lg2_approx(pacc[c]), sacc[c]);
+        float v = -sacc[c];
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
         if (lane == 0) red[quarter * CT + half * kCW + c] = (double)v;
