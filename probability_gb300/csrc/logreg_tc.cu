@@ -463,6 +463,404 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
   }
 }
 
+// ---------------------------------------------------------------------------
+// 256 < D <= 512: a cluster of two CTAs shares each (chain tile, row tile).
+//
+// One CTA cannot hold a 128-row X tile of 512 features (128 KB per stage)
+// beside the BF16 hi/lo chain states, so the features are split: CTA p of the
+// pair keeps features [256p, 256p + 256) of X and of the states and forms the
+// partial Z_p = X[:, F_p] B[:, F_p]^T in its TMEM.  Rows 64p .. 64p+63 belong
+// to CTA p: its "send" warps copy the partial of the other 64 rows into the
+// peer's exchange buffer (distributed shared memory), its "compute" warps add
+// the peer's partial to their own, run the epilogue and write R into both
+// CTAs' R tiles.  Each CTA then accumulates G for its own features,
+// G_p += X[:, F_p]^T R.  X is read from L2 once per chain tile, as in the
+// single-CTA kernel.  Every wait is bounded; a CTA that gives up also sets
+// its peer's abort flag.
+// ---------------------------------------------------------------------------
+constexpr int kPairKB = 4;                  // 64-feature blocks per CTA
+constexpr int kPairCT = 64;                 // chains per tile
+constexpr int kPairEpi = 16;                // epilogue warps (8 compute + 8 send)
+constexpr int kZxStride = kPairCT * 4 + 16; // bytes per exchange row (bank-conflict pad)
+
+struct PairLayout {
+  static constexpr int kXStage = kPairKB * 16384;           // [4][128 rows][128 B]
+  static constexpr int kBBytes = kPairKB * kPairCT * 128;   // [4][64 chains][128 B]
+  static constexpr int kRBuf = 16384;                       // [128 rows][64 chains] BF16
+  static constexpr int kX = 0;                              // 2 stages
+  static constexpr int kBhi = kX + 2 * kXStage;
+  static constexpr int kBlo = kBhi + kBBytes;
+  static constexpr int kR = kBlo + kBBytes;
+  static constexpr int kZx = kR + kRBuf;                    // [64 rows][kZxStride]
+  static constexpr int kCtl = kZx + 64 * kZxStride;
+  static constexpr int kBytes = kCtl + 256;
+  static_assert(kBytes + 1024 <= 232448, "shared memory over the sm_103a limit");
+};
+
+struct PairBars {
+  uint64_t x_full[2], x_empty[2], z_full[2], z_empty[2];
+  uint64_t zx_full;   // peer's partial for my rows has arrived (8 remote arrivals)
+  uint64_t zx_free;   // peer has read what I sent last (8 remote arrivals)
+  uint64_t r_full;    // R tile complete (8 local + 8 remote arrivals)
+  uint64_t r_free;    // both CTAs' GEMM2 done with R (2 multicast commits)
+  uint64_t g_done, drain;
+};
+
+__device__ __forceinline__ bool wait_cluster_or_abort(uint64_t* bar, uint32_t parity,
+                                                      volatile int* abort_flag) {
+  if (tc::mbar_try_wait_cluster(bar, parity)) return true;
+  const uint64_t t0 = tc::globaltimer_ns();
+  while (true) {
+    if (tc::mbar_try_wait_cluster(bar, parity)) return true;
+    if (*abort_flag) return false;
+    if (tc::globaltimer_ns() - t0 > kWaitLimitNs) return false;
+  }
+}
+
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads(kPairEpi), 1)
+logreg_tc_pair_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restrict__ y,
+                      int N, int D, const float* __restrict__ Q, int ldq,
+                      const int* __restrict__ n_dev, int pairs, double* __restrict__ lpart,
+                      float* __restrict__ gpart, int* __restrict__ err) {
+  using L = PairLayout;
+  constexpr int CT = kPairCT;
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int n = *n_dev;
+  const int row_tiles = (N + kRows - 1) / kRows;
+  const int S = tc_splits(n, CT, pairs, row_tiles);
+  const int tiles = (n + CT - 1) / CT;
+  const int pair = blockIdx.x >> 1;
+  // Both CTAs of a pair leave together (no cluster barrier is reached).
+  if (S == 0 || pair >= tiles * S) return;
+  const uint32_t p = tc::cluster_ctarank(), peer = p ^ 1u;
+  const int tile = pair % tiles, split = pair / tiles;
+  const int c0 = tile * CT;
+  const int rt_begin = (int)((long long)split * row_tiles / S);
+  const int rt_end = (int)((long long)(split + 1) * row_tiles / S);
+  const int T = rt_end - rt_begin;
+  const int f0 = 256 * (int)p;                        // first feature of this CTA
+  const int fD = min(256, D - f0);                    // features held (>= 1: D > 256)
+
+  unsigned char* Xs = smem + L::kX;
+  unsigned char* Bhi = smem + L::kBhi;
+  unsigned char* Blo = smem + L::kBlo;
+  unsigned char* Rs = smem + L::kR;
+  unsigned char* Zx = smem + L::kZx;
+  PairBars* bars = reinterpret_cast<PairBars*>(smem + L::kCtl);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::kCtl + sizeof(PairBars));
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+  auto abort_both = [&]() {
+    *abort_flag = 1;
+    tc::st_cluster_u32(tc::map_to_rank(tc::smem_u32((const void*)abort_flag), peer), 1u);
+  };
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  float lp_pub = 0.f;   // compute warps, lane j < 16: log-likelihood partial of chain 16 sub + j
+  if (tid == 0) {
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&bars->x_full[i], 1);
+      tc::mbar_init(&bars->x_empty[i], 1);
+      tc::mbar_init(&bars->z_full[i], 1);
+      tc::mbar_init(&bars->z_empty[i], kPairEpi);
+    }
+    tc::mbar_init(&bars->zx_full, 8);
+    tc::mbar_init(&bars->zx_free, 8);
+    tc::mbar_init(&bars->r_full, 16);
+    tc::mbar_init(&bars->r_free, 2);
+    tc::mbar_init(&bars->g_done, 1);
+    tc::mbar_init(&bars->drain, 1);
+    *abort_flag = 0;
+    tc::fence_mbar_init();
+    tc::prefetch_tmap(&xmap);
+  }
+  if (warp == 1) tc::tmem_alloc(tmem_slot, 256);
+
+  // This CTA's feature half of the chain states / 2 -> BF16 hi/lo, K-major
+  // 128-byte-swizzled [4][CT][128 B] (h = z / 2 in the accumulator).
+  for (int i = tid; i < CT * kPairKB * 8; i += tc_threads(kPairEpi)) {
+    const int c = i / (kPairKB * 8), chunk = i % (kPairKB * 8);
+    const int d0 = chunk * 8;
+    float v[8];
+#pragma unroll
+    for (int e = 0; e < 8; ++e) {
+      const int d = f0 + d0 + e;
+      v[e] = (c0 + c < n && d < D) ? 0.5f * Q[(size_t)(c0 + c) * ldq + d] : 0.f;
+    }
+    uint32_t hi[4], lo[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+      const __nv_bfloat162 h = __floats2bfloat162_rn(v[2 * e], v[2 * e + 1]);
+      hi[e] = *reinterpret_cast<const uint32_t*>(&h);
+      const float2 hf = __bfloat1622float2(h);
+      lo[e] = pack_bf16x2(v[2 * e] - hf.x, v[2 * e + 1] - hf.y);
+    }
+    const uint32_t off = (d0 >> 6) * (CT * 128) + tc::sw128_offset(c, d0 & 63);
+    *reinterpret_cast<uint4*>(Bhi + off) = make_uint4(hi[0], hi[1], hi[2], hi[3]);
+    *reinterpret_cast<uint4*>(Blo + off) = make_uint4(lo[0], lo[1], lo[2], lo[3]);
+  }
+  tc::fence_proxy_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  // The peer's barriers are initialised before anyone arrives on them.
+  tc::cluster_sync();
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    // ---------------- TMA producer: X[rows, F_p] ----------------
+    if (lane == 0) {
+      int it = 0;
+      for (; it < T; ++it) {
+        const int s = it & 1;
+        if (!wait_or_abort(&bars->x_empty[s], ((uint32_t)(it >> 1) & 1) ^ 1, abort_flag)) {
+          tc::record_error(err, kTcTimeoutTma);
+          abort_both();
+          break;
+        }
+        tc::mbar_arrive_expect_tx(&bars->x_full[s], L::kXStage);
+#pragma unroll
+        for (int kb = 0; kb < kPairKB; ++kb)
+          tc::tma_load_2d(Xs + s * L::kXStage + kb * 16384, &xmap, f0 + kb * 64,
+                          (rt_begin + it) * kRows, &bars->x_full[s]);
+      }
+      for (int j = (it > 2 ? it - 2 : 0); j < it; ++j)
+        tc::mbar_wait(&bars->x_full[j & 1], (uint32_t)((j >> 1) & 1), kWaitLimitNs);
+    }
+    __syncwarp();
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      constexpr uint32_t idesc1 = tc::idesc_bf16_f32(128, CT, false, false);
+      constexpr uint32_t idesc2 = tc::idesc_bf16_f32(128, CT, true, true);
+      const uint32_t xs_a = tc::smem_u32(Xs), bhi_a = tc::smem_u32(Bhi);
+      const uint32_t blo_a = tc::smem_u32(Blo), rs_a = tc::smem_u32(Rs);
+      const uint32_t tg = tmem + 2 * CT;
+      const int ksteps = (fD + 15) >> 4;        // K-steps of 16 features holding data
+      const int mtiles = (fD + 127) >> 7;       // 128-feature tiles of G
+      bool ok = true;
+      auto gemm1 = [&](int it) -> bool {
+        const int s = it & 1, b = it & 1;
+        const uint32_t use = (uint32_t)(it >> 1) & 1;
+        if (!wait_or_abort(&bars->x_full[s], use, abort_flag)) return false;
+        if (!wait_or_abort(&bars->z_empty[b], use ^ 1, abort_flag)) return false;
+        tc::tc_fence_after();
+        const uint32_t tz = tmem + b * CT;
+        const uint32_t xa = xs_a + s * L::kXStage;
+#pragma unroll
+        for (int kb = 0; kb < kPairKB; ++kb) {
+#pragma unroll
+          for (int k = 0; k < 4; ++k) {
+            if (kb * 4 + k >= ksteps) break;
+            const uint64_t a = tc::smem_desc_sw128(xa + kb * 16384 + k * 32, 16, 1024);
+            const uint64_t bh = tc::smem_desc_sw128(bhi_a + kb * (CT * 128) + k * 32, 16, 1024);
+            const uint64_t bl = tc::smem_desc_sw128(blo_a + kb * (CT * 128) + k * 32, 16, 1024);
+            tc::mma_bf16(tz, a, bh, idesc1, (kb | k) ? 1u : 0u);
+            tc::mma_bf16(tz, a, bl, idesc1, 1u);
+          }
+        }
+        tc::mma_commit(&bars->z_full[b]);
+        return true;
+      };
+      if (T > 0) ok = gemm1(0);
+      for (int it = 0; it < T && ok; ++it) {
+        if (it + 1 < T) {
+          ok = gemm1(it + 1);
+          if (!ok) break;
+        }
+        if (!wait_cluster_or_abort(&bars->r_full, (uint32_t)it & 1, abort_flag)) {
+          ok = false;
+          break;
+        }
+        tc::tc_fence_after();
+        const uint32_t xa = xs_a + (it & 1) * L::kXStage;
+        for (int mt = 0; mt < mtiles; ++mt) {
+#pragma unroll
+          for (int ks = 0; ks < kRows / 16; ++ks) {
+            const uint64_t a = tc::smem_desc_sw128(xa + mt * 32768 + ks * 2048, 16384, 1024);
+            const uint64_t bd = tc::smem_desc_sw128(rs_a + ks * 2048, 16384, 1024);
+            tc::mma_bf16(tg + mt * CT, a, bd, idesc2, (it > 0 || ks > 0) ? 1u : 0u);
+          }
+        }
+        tc::mma_commit(&bars->x_empty[it & 1]);
+        tc::mma_commit_multicast(&bars->r_free, (uint16_t)0x3);
+      }
+      if (ok) {
+        tc::mma_commit(&bars->g_done);
+      } else {
+        tc::record_error(err, kTcTimeoutMma);
+        abort_both();
+      }
+      tc::mma_commit(&bars->drain);
+      tc::mbar_wait(&bars->drain, 0, kWaitLimitNs);
+    }
+    __syncwarp();
+  } else {
+    // ---------------- epilogue: 8 compute + 8 send warps ----------------
+    // (waits are made warp-uniform so that no lane leaves a loop alone)
+    const int quarter = warp & 3;                 // TMEM lanes (rows) 32*quarter ..
+    const int sub = (warp - 2) >> 2;              // chains [16 sub, 16 sub + 16)
+    const bool compute = (quarter >> 1) == (int)p;  // rows 64p .. 64p+63 are mine
+    const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+    const int r = quarter * 32 + lane;            // row of the tile (TMEM lane)
+    const int xrow = (quarter & 1) * 32 + lane;   // row in the 64-row exchange buffer
+    const uint32_t zx_peer = tc::map_to_rank(tc::smem_u32(Zx), peer) + xrow * kZxStride + sub * 64;
+    const uint32_t r_off = tc::sw128_offset(r, sub * 16);
+    const uint32_t r_off8 = tc::sw128_offset(r, sub * 16 + 8);
+    const uint32_t r_peer = tc::map_to_rank(tc::smem_u32(Rs), peer);
+    const uint32_t zx_full_peer = tc::map_to_rank(tc::smem_u32(&bars->zx_full), peer);
+    const uint32_t zx_free_peer = tc::map_to_rank(tc::smem_u32(&bars->zx_free), peer);
+    const uint32_t r_full_peer = tc::map_to_rank(tc::smem_u32(&bars->r_full), peer);
+    float sacc[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) sacc[c] = 0.f;
+    bool ok = true;
+    float y_next = 0.f;
+    if (compute) {
+      const int row0 = rt_begin * kRows + r;
+      if (T > 0 && row0 < N) y_next = y[row0];
+    }
+    for (int it = 0; it < T; ++it) {
+      const int b = it & 1;
+      const uint32_t ph = (uint32_t)it & 1;
+      if (!__all_sync(0xffffffffu, wait_or_abort(&bars->z_full[b], (uint32_t)(it >> 1) & 1, abort_flag))) {
+        ok = false;
+        break;
+      }
+      tc::tc_fence_after();
+      float h[16];
+      tc::tmem_ld16(tmem + b * CT + sub * 16 + lane_base, h);
+      tc::tmem_ld_wait();
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&bars->z_empty[b]);
+      if (!compute) {
+        // Send the partial of the peer's rows.
+        if (!__all_sync(0xffffffffu, wait_cluster_or_abort(&bars->zx_free, ph ^ 1, abort_flag))) {
+          ok = false;
+          break;
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+          tc::st_cluster_v4(zx_peer + 16 * j,
+                            make_uint4(__float_as_uint(h[4 * j]), __float_as_uint(h[4 * j + 1]),
+                                       __float_as_uint(h[4 * j + 2]),
+                                       __float_as_uint(h[4 * j + 3])));
+        tc::fence_acq_rel_cluster();
+        __syncwarp();
+        if (lane == 0) tc::mbar_arrive_cluster(zx_full_peer);
+        continue;
+      }
+      // Compute warp: add the peer's partial for this row.
+      if (!__all_sync(0xffffffffu, wait_cluster_or_abort(&bars->zx_full, ph, abort_flag))) {
+        ok = false;
+        break;
+      }
+      const float4* zx = reinterpret_cast<const float4*>(Zx + xrow * kZxStride + sub * 64);
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const float4 v = zx[j];
+        h[4 * j] += v.x;
+        h[4 * j + 1] += v.y;
+        h[4 * j + 2] += v.z;
+        h[4 * j + 3] += v.w;
+      }
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive_cluster(zx_free_peer);
+      const int row = (rt_begin + it) * kRows + r;
+      const bool valid = row < N;
+      const float ym = (valid ? y_next : 0.f) - 0.5f;
+      if (it + 1 < T && row + kRows < N) y_next = y[row + kRows];
+      uint32_t rp[8] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+      if (valid) {
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const float a = fabsf(h[j]);
+          const float t = tc::ex2_approx(a * kNeg2Log2e);       // e^-|z|
+          sacc[j] += fmaf(kLn2, tc::lg2_approx(1.f + t), a);
+        }
+#pragma unroll
+        for (int j = 0; j < 8; ++j) rp[j] = residual_bf16x2(h[2 * j], h[2 * j + 1], ym);
+      }
+      // Both CTAs' GEMM2 of the previous tile must be done with R.
+      if (!__all_sync(0xffffffffu, wait_cluster_or_abort(&bars->r_free, ph ^ 1, abort_flag))) {
+        ok = false;
+        break;
+      }
+      const uint4 v0 = make_uint4(rp[0], rp[1], rp[2], rp[3]);
+      const uint4 v1 = make_uint4(rp[4], rp[5], rp[6], rp[7]);
+      *reinterpret_cast<uint4*>(Rs + r_off) = v0;
+      *reinterpret_cast<uint4*>(Rs + r_off8) = v1;
+      tc::st_cluster_v4(r_peer + r_off, v0);
+      tc::st_cluster_v4(r_peer + r_off8, v1);
+      tc::fence_proxy_async_smem();
+      tc::fence_proxy_async_cluster();
+      tc::fence_acq_rel_cluster();
+      __syncwarp();
+      if (lane == 0) {
+        tc::mbar_arrive(&bars->r_full);
+        tc::mbar_arrive_cluster(r_full_peer);
+      }
+    }
+    if (ok && T > 0) ok = __all_sync(0xffffffffu, wait_or_abort(&bars->g_done, 0, abort_flag));
+    if (!ok) {
+      tc::record_error(err, kTcTimeoutEpilogue);
+      abort_both();
+    } else {
+      tc::tc_fence_after();
+      // G_p: TMEM lane = feature (of this CTA's half), column = chain.
+      for (int mt = 0; mt * 128 < fD; ++mt) {
+        const int d = f0 + mt * 128 + quarter * 32 + lane;
+        float g[16];
+        tc::tmem_ld16(tmem + 2 * CT + mt * CT + sub * 16 + lane_base, g);
+        tc::tmem_ld_wait();
+        if (d < D) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int c = c0 + sub * 16 + j;
+            if (c < n) gpart[((size_t)split * n + c) * D + d] = g[j];
+          }
+        }
+      }
+    }
+    if (compute) {
+      // Nonlinear log-likelihood partial of this warp's 32 rows, per chain,
+      // into red[p][quarter & 1][chain] of CTA 0 (the exchange buffer is idle
+      // after the loop; both CTAs have finished it at the cluster barrier).
+#pragma unroll
+      for (int j = 0; j < 16; ++j) {
+        float v = -sacc[j];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (j == lane) lp_pub = v;
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::cluster_sync();
+  if (warp >= 2 && ((warp & 3) >> 1) == (int)p && lane < 16) {
+    const int sub = (warp - 2) >> 2;
+    const int slot = ((int)p * 2 + (warp & 1)) * CT + sub * 16 + lane;
+    const uint32_t dst = tc::map_to_rank(tc::smem_u32(Zx), 0) + slot * 8;
+    const double dv = (double)lp_pub;
+    asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(dst), "d"(dv) : "memory");
+  }
+  tc::cluster_sync();
+  if (p == 0 && !*abort_flag) {
+    const double* red = reinterpret_cast<const double*>(Zx);
+    for (int c = tid; c < CT; c += tc_threads(kPairEpi)) {
+      const double sum = red[c] + red[CT + c] + red[2 * CT + c] + red[3 * CT + c];
+      if (c0 + c < n) lpart[(size_t)split * n + c0 + c] = sum;
+    }
+  }
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, 256);
+  }
+}
+
 // FP32 X -> X_hi = bf16(X) and (optionally) X_lo = bf16(X - X_hi), zero-padded
 // to Dp features.
 __global__ void to_bf16_padded(const float* __restrict__ X, int64_t N, int D, int Dp,
@@ -541,7 +939,7 @@ class LogregTc final : public Target {
            float prior_scale)
       : N_(n), D_(d) {
     dim = d;
-    kb_ = d <= 128 ? 2 : 4;
+    kb_ = d <= 128 ? 2 : d <= 256 ? 4 : 8;   // 8: the pair-cluster kernel
     ct_ = kb_ == 2 ? 128 : 64;
     // FP32 data up to 128 features keeps a BF16 residual X_lo (see XLO).
     xlo_ = (x_dtype == 0 && kb_ == 2);
@@ -585,6 +983,19 @@ class LogregTc final : public Target {
     inv_var_ = 1.f / (prior_scale * prior_scale);
     log_norm_ = -log((double)prior_scale) - 0.5 * log(2.0 * M_PI);
     grid_ = ctx->num_sms;
+    if (kb_ == 8) {
+      // grid_ counts CTA pairs: as many 2-CTA clusters as can be resident.
+      smem_ = PairLayout::kBytes + 1024;
+      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_pair_kernel,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_));
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(2 * (ctx->num_sms / 2));
+      cfg.blockDim = dim3(tc_threads(kPairEpi));
+      cfg.dynamicSmemBytes = smem_;
+      int clusters = 0;
+      GBM_CUDA(cudaOccupancyMaxActiveClusters(&clusters, logreg_tc_pair_kernel, &cfg));
+      grid_ = std::max(1, std::min(ctx->num_sms / 2, clusters));
+    }
     encode(&xmap_, xb_.ptr, Dp);
     encode(&xlomap_, xlo_ ? xl_.ptr : xb_.ptr, Dp);
     const int attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
@@ -596,7 +1007,7 @@ class LogregTc final : public Target {
       smem_ = TcLayout<2, 128, false>::kBytes + 1024;
       GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<2, 128, 16, false>, (cudaFuncAttribute)attr,
                                     (int)smem_));
-    } else {
+    } else if (kb_ == 4) {
       smem_ = TcLayout<4, 64, false>::kBytes + 1024;
       GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<4, 64, 8, false>, (cudaFuncAttribute)attr,
                                     (int)smem_));
@@ -619,7 +1030,10 @@ class LogregTc final : public Target {
       xmap_, xlomap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_dev_)
     if (kb_ == 2 && xlo_) GBM_TC_LAUNCH(2, 128, 16, true);
     else if (kb_ == 2) GBM_TC_LAUNCH(2, 128, 16, false);
-    else GBM_TC_LAUNCH(4, 64, 8, false);
+    else if (kb_ == 4) GBM_TC_LAUNCH(4, 64, 8, false);
+    else
+      logreg_tc_pair_kernel<<<2 * grid_, tc_threads(kPairEpi), smem_, s>>>(
+          xmap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_dev_);
 #undef GBM_TC_LAUNCH
     GBM_CUDA(cudaGetLastError());
     launch_split_reduce(lpart, gpart, q, ldq, n_dev, cap, ct_, kRows, grid_, N, D, inv_var_,
@@ -664,7 +1078,7 @@ class LogregTc final : public Target {
 
 std::unique_ptr<Target> make_logreg_tc(gbm_context* ctx, const void* X, int x_dtype, int64_t n,
                                        int64_t d, const float* y, float prior_scale) {
-  if (d > 256) return nullptr;
+  if (d > 512) return nullptr;
   return std::unique_ptr<Target>(new LogregTc(ctx, X, x_dtype, n, d, y, prior_scale));
 }
 

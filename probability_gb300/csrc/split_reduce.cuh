@@ -5,7 +5,7 @@
 // gpart[S][n][D] (float32), where S = number of row splits for n chains:
 //   S = clamp(grid / ceil(n / ct), 1, ceil(N / nt)).
 // One CTA per chain: warp w sums splits w, w + W, w + 2W, ... (each lane
-// owns features lane + 32k, D <= 256), then the W partial sums are combined
+// owns features lane + 32k, D <= 512), then the W partial sums are combined
 // in warp order.  The order depends only on S, so results are reproducible;
 // with many splits (few chains) all W warps keep loads in flight.
 //
@@ -33,6 +33,7 @@ __device__ __forceinline__ int split_count(int n, int ct, int nt, int grid, int 
   return s > row_tiles ? row_tiles : s;
 }
 
+template <int DMAX>
 __global__ void __launch_bounds__(32 * kReduceWarps)
 split_reduce_kernel(const double* __restrict__ lpart, const float* __restrict__ gpart,
                     const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev, int ct,
@@ -44,23 +45,26 @@ split_reduce_kernel(const double* __restrict__ lpart, const float* __restrict__ 
   if (c >= n) return;
   const int S = split_count(n, ct, nt, grid, N);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  __shared__ float gsum[kReduceWarps][256];
+  __shared__ float gsum[kReduceWarps][DMAX];
   __shared__ double lsum[kReduceWarps];
   __shared__ double prior_s;
   const size_t sstride = (size_t)n * D;
   const float* p = gpart + (size_t)c * D;
-  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  constexpr int kK = DMAX / 32;
+  float acc[kK];
+#pragma unroll
+  for (int k = 0; k < kK; ++k) acc[k] = 0.f;
   double lp = 0.0;
   for (int s = warp; s < S; s += kReduceWarps) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < kK; ++k) {
       const int d = lane + 32 * k;
       if (d < D) acc[k] += p[(size_t)s * sstride + d];
     }
     if (lane == 0) lp += lpart[(size_t)s * n + c];
   }
 #pragma unroll
-  for (int k = 0; k < 8; ++k) gsum[warp][lane + 32 * k] = acc[k];
+  for (int k = 0; k < kK; ++k) gsum[warp][lane + 32 * k] = acc[k];
   if (lane == 0) lsum[warp] = lp;
   if (warp == 0) {
     double pr = 0.0, li = 0.0;
@@ -92,9 +96,12 @@ void launch_split_reduce(const double* lpart, const float* gpart, const float* Q
                          const int* n_dev, int cap, int ct, int nt, int grid, int N, int D,
                          float inv_var, double log_norm, const double* lin, double* logp,
                          float* grad, int ldg, cudaStream_t s) {
-  split_reduce_kernel<<<cap, 32 * kReduceWarps, 0, s>>>(lpart, gpart, Q, ldq, n_dev, ct, nt, grid,
-                                                       N, D, inv_var, log_norm, lin, logp, grad,
-                                                       ldg);
+  if (D <= 256)
+    split_reduce_kernel<256><<<cap, 32 * kReduceWarps, 0, s>>>(
+        lpart, gpart, Q, ldq, n_dev, ct, nt, grid, N, D, inv_var, log_norm, lin, logp, grad, ldg);
+  else
+    split_reduce_kernel<512><<<cap, 32 * kReduceWarps, 0, s>>>(
+        lpart, gpart, Q, ldq, n_dev, ct, nt, grid, N, D, inv_var, log_norm, lin, logp, grad, ldg);
   GBM_CUDA(cudaGetLastError());
 }
 

@@ -31,7 +31,10 @@ def _bf16_round(x):
 
 
 @pytest.mark.parametrize('n,d,c', [(1000, 25, 64), (5000, 100, 300), (3000, 200, 70),
-                                   (130, 7, 1), (4096, 128, 128), (777, 250, 129)])
+                                   (130, 7, 1), (4096, 128, 128), (777, 250, 129),
+                                   # 256 < D <= 512: the pair-cluster kernel
+                                   (3000, 300, 70), (777, 512, 129), (2000, 257, 64),
+                                   (5000, 400, 300), (129, 511, 1)])
 def test_mixed_log_prob_and_grad_vs_fp64(pg, n, d, c):
   X, y, _ = _problems.logreg_data(n, d, seed=n + 7 * d, scale=1.0 / np.sqrt(d))
   Xb = torch.from_numpy(X).to(torch.bfloat16)
