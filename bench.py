@@ -37,21 +37,103 @@ WORKLOADS = {
                                 feature_scale=0.1, step0=0.1, target_accept=0.8,
                                 num_adaptation_steps=1000, precision='mixed'),
 }
+# Mixed precision at scale: X 1e6 x 512 BF16, 4096 chains, NUTS depth 8.
+WORKLOADS['nuts_logreg_1e6x512_bf16'] = dict(n=1000000, d=512, chains=4096, depth=8, seed=2,
+                                             feature_scale=512 ** -0.5, step0=0.01,
+                                             target_accept=0.8, num_adaptation_steps=1000,
+                                             precision='mixed', x_dtype='bf16',
+                                             precision_report=10000)
 WORKLOADS['hmc_logreg_1000x25'] = dict(n=1000, d=25, chains=64, seed=0, feature_scale=1.0,
                                        step0=0.03, leapfrogs=10, burnin=500, precision='fp32')
+# Serving: a Poisson(200/s) stream of DA(NUTS) logistic-regression jobs, each
+# with N ~ log-U[1e3, 2e5] rows, D ~ log-U[10, 1000] features (BF16 X, N(0,
+# 1/D), intercept column), 16-256 chains, 500-5000 draws after 300
+# adaptation steps, admitted under a 150 GB device-memory budget.  The timed
+# sample is the first `requests` jobs of the stream; draws and adaptation
+# steps are multiplied by `length_scale`, and D is capped at the mixed
+# path's 512 features (both stated in the output).
+WORKLOADS['serve_logreg_stream'] = dict(rate=200.0, requests=64, length_scale=0.1, seed=4,
+                                        n_range=(1e3, 2e5), d_range=(10, 1000), d_cap=512,
+                                        chains=(16, 256), draws=(500, 5000), adapt=300,
+                                        depth=10, budget_gb=150, workers=16)
 METRIC = 'grad-evals/s (NUTS leapfrogs_taken summed over chains; min-ESS/s reported beside)'
 METRIC_HMC = 'grad-evals/s (HMC: chains x num_leapfrog_steps per transition; min-ESS/s beside)'
 
 
 def make_data(w):
   rng = np.random.default_rng(w['seed'])
-  X = rng.normal(size=(w['n'], w['d'])) * w['feature_scale']
+  if w['n'] * w['d'] > 5e7:   # large: draw in float32 directly
+    X = rng.standard_normal((w['n'], w['d']), dtype=np.float32)
+    X *= np.float32(w['feature_scale'])
+  else:
+    X = rng.normal(size=(w['n'], w['d'])) * w['feature_scale']
   X[:, 0] = 1.0
   beta = rng.normal(size=w['d'])
-  p = 1.0 / (1.0 + np.exp(-(X @ beta)))
+  p = 1.0 / (1.0 + np.exp(-(X @ beta.astype(X.dtype))))
   y = (rng.uniform(size=w['n']) < p).astype(np.float32)
   init = (rng.normal(size=(w['chains'], w['d'])) * 0.1).astype(np.float32)
   return X.astype(np.float32), y, init
+
+
+def engine_features(X, w):
+  """X as the engine receives it: BF16 for the BF16-data workloads."""
+  import torch
+  Xt = torch.from_numpy(X)
+  return Xt.to(torch.bfloat16) if w.get('x_dtype') == 'bf16' else Xt
+
+
+def cpu_gradient_rate(X, y, q, max_seconds):
+  """grad-evals/s of the oracle's batched log-density + gradient (NumPy float32,
+  all host threads) on the chains of `q`: the per-leaf cost of NUTS, for
+  workloads where one CPU transition would take minutes."""
+  Xf = X.astype(np.float32)
+  yf = y.astype(np.float32)
+  evals = 0
+  t0 = time.perf_counter()
+  while True:
+    z = q @ Xf.T
+    sp = np.logaddexp(np.float32(0), z)
+    lp = (yf * z - sp).sum(-1, dtype=np.float64)
+    g = (yf - np.exp(z - sp)) @ Xf - q
+    evals += q.shape[0]
+    if time.perf_counter() - t0 > max_seconds:
+      break
+  del lp, g
+  dt = time.perf_counter() - t0
+  return evals / dt, evals // q.shape[0], dt
+
+
+def precision_report(target, X_engine, y, n_states, seed, dev):
+  """Engine log-density and gradient against float64 arithmetic on the same
+  (BF16) data at n_states random states ~ N(0, I): relative error of the
+  log-density and gradient error relative to max |gradient|."""
+  import torch
+  g = torch.Generator(device=dev)
+  g.manual_seed(seed)
+  N, D = X_engine.shape
+  X64 = X_engine.to(dev).to(torch.float64)
+  y64 = torch.as_tensor(y, device=dev, dtype=torch.float64)
+  lp_err, g_err = [], []
+  chunk, rows = 1000, 100000
+  for s0 in range(0, n_states, chunk):
+    q = torch.randn(min(chunk, n_states - s0), D, device=dev, generator=g)
+    lp, gr = target.log_prob_and_grad(q)
+    q64 = q.to(torch.float64)
+    lp64 = -0.5 * (q64 * q64).sum(-1) - 0.5 * D * np.log(2 * np.pi)
+    g64 = -q64.clone()
+    for r0 in range(0, N, rows):
+      z = X64[r0:r0 + rows] @ q64.T
+      yy = y64[r0:r0 + rows, None]
+      lp64 += (yy * z - torch.nn.functional.softplus(z)).sum(0)
+      g64 += (yy - torch.sigmoid(z)).T @ X64[r0:r0 + rows]
+    lp_err.append(((lp - lp64).abs() / lp64.abs()).cpu())
+    g_err.append(((gr.to(torch.float64) - g64).abs().amax(-1) / g64.abs().amax(-1)).cpu())
+  lp_err = torch.cat(lp_err)
+  g_err = torch.cat(g_err)
+  return {'states': n_states, 'reference': 'float64 on the GPU, same BF16 X',
+          'log_prob_rel_err_max': float(lp_err.max()), 'log_prob_rel_err_median':
+          float(lp_err.median()), 'grad_err_rel_to_max_abs_grad_max': float(g_err.max()),
+          'grad_err_rel_to_max_abs_grad_median': float(g_err.median())}
 
 
 class ClockSampler:
@@ -115,12 +197,13 @@ def read_peaks():
     return {'hbm_gbs': 6800.0, 'bf16_tflops': 1900.0, 'bf16_tflops_sustained': 1700.0}, 'fallback'
 
 
-def read_traffic(kernel_name):
-  """Per-launch DRAM traffic of the dominant kernel from the committed ncu
-  summary (profiles/traffic.json), if one was captured for this kernel."""
+def read_traffic(workload, kernel_name):
+  """Per-launch DRAM traffic (bytes read + written) of the dominant kernel at
+  the full chain batch, from the committed ncu summary
+  (profiles/traffic.json, keyed 'workload/kernel'), if one was captured."""
   try:
     t = json.load(open(os.path.join(ROOT, 'profiles', 'traffic.json')))
-    return t.get(kernel_name)
+    return t.get('%s/%s' % (workload, kernel_name))
   except (OSError, ValueError):
     return None
 
@@ -200,7 +283,8 @@ def run_kernel_only(args, w):
   import torch
   import probability_gb300 as pg
   X, y, init = make_data(w)
-  target = pg.LogisticRegression(X, y, precision=args.precision or w['precision'])
+  target = pg.LogisticRegression(engine_features(X, w), y,
+                                 precision=args.precision or w['precision'])
   q = torch.from_numpy(init).cuda()
   for _ in range(args.warmup):
     target.log_prob_and_grad(q)
@@ -272,7 +356,8 @@ def run_engine(args, w):
   if world > 1:  # independent replicas: per-rank init state
     init = (np.random.default_rng(w['seed'] + 100 * rank).normal(size=init.shape) * 0.1
             ).astype(np.float32)
-  target = pg.LogisticRegression(X, y, precision=args.precision or w['precision'])
+  X_engine = engine_features(X, w)
+  target = pg.LogisticRegression(X_engine, y, precision=args.precision or w['precision'])
   nuts = pg.mcmc.NoUTurnSampler(target, step_size=w['step0'], max_tree_depth=w['depth'])
   kernel = pg.mcmc.DualAveragingStepSizeAdaptation(
       nuts, num_adaptation_steps=w['num_adaptation_steps'],
@@ -353,11 +438,12 @@ def run_engine(args, w):
   eval_s = eval_ms.value / 1000.0
   achieved_tflops = alg_flops / eval_s / 1e12 if eval_s > 0 else None
   tensor_peak = peaks['bf16_tflops']
-  kernel_name = 'logreg_partial_kernel' if target.precision == 'fp32' else 'logreg_tc_kernel'
+  kernel_name = ('logreg_partial_kernel' if target.precision == 'fp32' else
+                 'logreg_tc_pair_kernel' if w['d'] > 256 else 'logreg_tc_kernel')
   roofline = {
       'bound': 'tensor', 'achieved': achieved_tflops, 'peak': tensor_peak, 'unit': 'TFLOP/s',
       'frac': achieved_tflops / tensor_peak if achieved_tflops else None,
-      'traffic': read_traffic(kernel_name), 'kernel': kernel_name,
+      'traffic': read_traffic(args.workload, kernel_name), 'kernel': kernel_name,
       'peak_source': peak_src + ' (MEASURED_PEAKS.json bf16_tflops burst)',
       'eval_launches': int(evals.value), 'eval_ms_total': eval_ms.value,
       'alg_flops_per_grad_eval': flops_per_grad,
@@ -406,7 +492,9 @@ def run_engine(args, w):
 
   # ---- the plain FP32 form on the same GPU, from the same adapted state ----
   plain = None
-  if target.precision != 'fp32' and args.plain_steps > 0:
+  if w['d'] > 256:
+    plain = {'value': None, 'note': 'the FP32 CUDA-core target supports up to 256 features'}
+  elif target.precision != 'fp32' and args.plain_steps > 0:
     t32 = pg.LogisticRegression(X, y, precision='fp32')
     eps = kr.new_step_size.reshape(-1)[0].item()
     n32 = pg.mcmc.NoUTurnSampler(t32, step_size=eps, max_tree_depth=w['depth'])
@@ -431,7 +519,15 @@ def run_engine(args, w):
                      'started from the same chain state'}
 
   cpu = None
-  if rank == 0 and world == 1 and not args.no_cpu_baseline:
+  if rank == 0 and world == 1 and not args.no_cpu_baseline and w['n'] * w['d'] > 5e7:
+    budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '20'))
+    sub = 64
+    rate, nev, dt = cpu_gradient_rate(X, y, state[:sub].cpu().numpy(), budget)
+    cpu = {'value': rate, 'unit': 'grad-evals/s', 'cores': os.cpu_count(), 'kind': 'port',
+           'sample': '%d batched log-prob+gradient evaluations of %d of the %d chains '
+                     '(%.1f s; the NUTS leaf cost, no tree bookkeeping); NumPy float32, '
+                     'BLAS threads = all cores' % (nev, sub, w['chains'], dt)}
+  elif rank == 0 and world == 1 and not args.no_cpu_baseline:
     budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '20'))
     sub = 64
     rate, nsteps, dt = cpu_baseline_run(w, X, y, init, budget, 1000000,
@@ -442,6 +538,10 @@ def run_engine(args, w):
                      'engine\'s adapted state and step size (%.1f s); NumPy float32 oracle, '
                      'chains in lock-step as in the reference, BLAS threads = all cores'
                      % (nsteps, sub, w['chains'], dt)}
+
+  prec = None
+  if rank == 0 and w.get('precision_report'):
+    prec = precision_report(target, X_engine, y, w['precision_report'], w['seed'], dev)
 
   if rank == 0:
     line = {
@@ -466,13 +566,107 @@ def run_engine(args, w):
         'roofline': roofline,
         'cpu_baseline': cpu,
         'plain_fp32': plain,
-        'speedup_vs_plain_fp32': (value / plain['value']) if plain else None,
+        'speedup_vs_plain_fp32': (value / plain['value']) if plain and plain['value'] else None,
         'gpu_launches': int(launches.value) + args.steps,
         'clocks': clk,
     }
+    if prec is not None:
+      line['precision_vs_fp64'] = prec
     print(json.dumps(line), flush=True)
   if dist is not None:
     dist.destroy_process_group()
+
+
+def run_serving(args, w):
+  """Replay the head of a Poisson request stream through the job server and
+  report latency percentiles, aggregate min-ESS/s and device throughput."""
+  import torch
+  import probability_gb300 as pg
+  from probability_gb300.serving import Server, DONE
+  world, rank, local = dist_setup(args)
+  if rank != 0:
+    return
+  dev = torch.device('cuda', local)
+  torch.cuda.set_device(dev)
+  rng = np.random.default_rng(w['seed'])
+  R = int(os.environ.get('GBM_SERVE_REQUESTS', w['requests']))
+  scale = w['length_scale']
+  jobs_spec = []
+  t_arr = 0.0
+  for i in range(R):
+    t_arr += rng.exponential(1.0 / w['rate'])
+    n = int(np.exp(rng.uniform(np.log(w['n_range'][0]), np.log(w['n_range'][1]))))
+    d_draw = int(np.exp(rng.uniform(np.log(w['d_range'][0]), np.log(w['d_range'][1]))))
+    c = int(rng.integers(w['chains'][0], w['chains'][1] + 1))
+    draws = int(rng.integers(w['draws'][0], w['draws'][1] + 1))
+    jobs_spec.append(dict(t=t_arr, n=n, d=min(d_draw, w['d_cap']), d_drawn=d_draw, c=c,
+                          draws=max(1, int(round(draws * scale))),
+                          adapt=max(1, int(round(w['adapt'] * scale))), seed=i))
+  # Data on the device before the clock starts (the server receives device
+  # pointers; generating X is not part of serving).
+  g = torch.Generator(device=dev)
+  g.manual_seed(w['seed'])
+  inputs = []
+  for js in jobs_spec:
+    X = torch.randn(js['n'], js['d'], device=dev, generator=g) * js['d'] ** -0.5
+    X[:, 0] = 1.0
+    beta = torch.randn(js['d'], device=dev, generator=g)
+    y = (torch.rand(js['n'], device=dev, generator=g) < torch.sigmoid(X @ beta)).float()
+    q0 = torch.randn(js['c'], js['d'], device=dev, generator=g) * 0.1
+    inputs.append((X.to(torch.bfloat16), y, q0))
+  torch.cuda.synchronize()
+  srv = Server(workers=w['workers'], memory_budget_bytes=int(w['budget_gb'] * 2**30),
+               device=local)
+  clocks = ClockSampler(local)
+  clocks.start()
+  handles = []
+  t0 = time.perf_counter()
+  srv_t0 = srv.now()
+  for js, (X, y, q0) in zip(jobs_spec, inputs):
+    delay = js['t'] - (time.perf_counter() - t0)
+    if delay > 0:
+      time.sleep(delay)
+    handles.append(srv.submit_logistic_regression(
+        X, y, q0, js['draws'], precision='mixed', num_burnin_steps=js['adapt'],
+        step_size=0.1, max_tree_depth=w['depth'], num_adaptation_steps=js['adapt'],
+        target_accept_prob=0.8, seed=(w['seed'], js['seed']),
+        trace=('state', 'leapfrogs_taken')))
+  infos = [h.wait(timeout=3600.0) for h in handles]
+  wall = time.perf_counter() - t0
+  clk = clocks.stop()
+  assert all(i['status'] == DONE for i in infos)
+  lat = np.array([i['end_s'] - i['submit_s'] for i in infos])
+  queue = np.array([i['start_s'] - i['submit_s'] for i in infos])
+  busy = max(i['end_s'] for i in infos) - min(i['submit_s'] for i in infos)
+  ess_sum, lf_sum, minstep = 0.0, 0, []
+  for h in handles:
+    st = h.states                       # [draws, C, D]
+    lf_sum += int(h.leapfrogs_taken.sum().item())
+    if st.shape[0] >= 4:
+      ess = pg.mcmc.effective_sample_size(st, filter_beyond_positive_pairs=True,
+                                          cross_chain_dims=1)
+      ess_sum += float(ess.min().item())
+  srv.close()
+  line = {
+      'metric': 'aggregate min-ESS/s over a served request stream (p50/p99 latency beside)',
+      'value': ess_sum / busy, 'unit': 'ESS/s', 'n_gpus': 1, 'steps': R, 'warmup': 0,
+      'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'bf16+f32',
+      'data': 'synthetic (seeded torch generator on the device)',
+      'config': {'workload': args.workload, 'arrival_rate_per_s': w['rate'], 'requests': R,
+                 'length_scale': scale, 'd_cap': w['d_cap'],
+                 'jobs_with_d_capped': int(sum(js['d_drawn'] > w['d_cap'] for js in jobs_spec)),
+                 'workers': w['workers'], 'memory_budget_gb': w['budget_gb'],
+                 'max_tree_depth': w['depth'],
+                 'note': 'the first %d requests of the Poisson stream; draws and adaptation '
+                         'steps x %.2f of the stated 500-5000 / 300' % (R, scale)},
+      'latency_s': {'p50': float(np.percentile(lat, 50)), 'p99': float(np.percentile(lat, 99)),
+                    'mean': float(lat.mean()), 'max': float(lat.max())},
+      'queue_s': {'p50': float(np.percentile(queue, 50)), 'p99': float(np.percentile(queue, 99))},
+      'makespan_s': busy, 'wall_s': wall, 'jobs_per_s': R / busy,
+      'grad_evals_per_s': lf_sum / busy,
+      'clocks': clk,
+  }
+  print(json.dumps(line), flush=True)
 
 
 def main():
@@ -498,6 +692,8 @@ def main():
     run_kernel_only(args, w)
   elif args.workload.startswith('hmc_'):
     run_hmc(args, w)
+  elif args.workload.startswith('serve_'):
+    run_serving(args, w)
   else:
     run_engine(args, w)
 
