@@ -282,6 +282,8 @@ def run_kernel_only(args, w):
   """Time the batched gradient alone at the full chain batch (profiling aid)."""
   import torch
   import probability_gb300 as pg
+  if args.kernel_rows:   # a smaller case of the same shape (profiling)
+    w = dict(w, n=args.kernel_rows)
   X, y, init = make_data(w)
   target = pg.LogisticRegression(engine_features(X, w), y,
                                  precision=args.precision or w['precision'])
@@ -684,6 +686,8 @@ def main():
                   help='transitions of the plain FP32 form timed beside the mixed path')
   ap.add_argument('--kernel-only', action='store_true',
                   help='time the batched log-prob+gradient alone (profiling aid)')
+  ap.add_argument('--kernel-rows', type=int, default=0,
+                  help='with --kernel-only: rows of X (default: the workload\'s)')
   args = ap.parse_args()
   w = WORKLOADS[args.workload]
   if args.impl == 'reference':

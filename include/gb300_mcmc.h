@@ -79,7 +79,10 @@ GBM_API int gbm_step_key(const uint32_t seed[2], uint64_t step, uint32_t out[2])
  * (mcmc/internal/util.py:286-308, math/gradient.py:28) for the
  * inference_gym logistic-regression target
  * (spinoffs/inference_gym/inference_gym/targets/logistic_regression.py:92-103,
- * distributions/bernoulli.py:126-140).  X and y are copied. */
+ * distributions/bernoulli.py:126-140).  X and y are copied.  Limits:
+ * num_features <= 256 for precision GBM_PRECISION_F32 (float32 X), <= 512 for
+ * GBM_PRECISION_MIXED (float32 or BF16 X; above 256 features a 2-CTA cluster
+ * shares each tile). */
 GBM_API int gbm_target_logistic_regression(gbm_context* ctx, const void* x, int x_dtype,
                                    int64_t num_rows, int64_t num_features, const float* y,
                                    float prior_scale, int precision, gbm_target** out);

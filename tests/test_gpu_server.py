@@ -106,7 +106,10 @@ def test_server_admission_respects_budget(pg):
 def test_server_rejects_bad_specs(pg):
   from probability_gb300.serving import Server
   srv = Server(workers=1, memory_budget_bytes=2**30)
-  X, y, _ = _problems.logreg_data(100, 300, seed=1)
-  with pytest.raises(ValueError):
-    srv.submit_logistic_regression(X, y, np.zeros((4, 300), np.float32), 2)
+  X, y, _ = _problems.logreg_data(100, 600, seed=1)
+  with pytest.raises(ValueError):   # beyond the mixed path's 512 features
+    srv.submit_logistic_regression(X, y, np.zeros((4, 600), np.float32), 2)
+  with pytest.raises(ValueError):   # beyond the FP32 path's 256 features
+    srv.submit_logistic_regression(X[:, :300], y, np.zeros((4, 300), np.float32), 2,
+                                   precision='fp32')
   srv.close()
