@@ -747,7 +747,8 @@ logreg_tc_pair_kernel(const __grid_constant__ CUtensorMap xmap, const float* __r
                             make_uint4(__float_as_uint(h[4 * j]), __float_as_uint(h[4 * j + 1]),
                                        __float_as_uint(h[4 * j + 2]),
                                        __float_as_uint(h[4 * j + 3])));
-        tc::fence_acq_rel_cluster();
+        // __syncwarp orders every lane's stores before lane 0's arrive, whose
+        // release (cluster scope) publishes them to the peer.
         __syncwarp();
         if (lane == 0) tc::mbar_arrive_cluster(zx_full_peer);
         continue;
@@ -796,7 +797,6 @@ logreg_tc_pair_kernel(const __grid_constant__ CUtensorMap xmap, const float* __r
       tc::st_cluster_v4(r_peer + r_off8, v1);
       tc::fence_proxy_async_smem();
       tc::fence_proxy_async_cluster();
-      tc::fence_acq_rel_cluster();
       __syncwarp();
       if (lane == 0) {
         tc::mbar_arrive(&bars->r_full);
