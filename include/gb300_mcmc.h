@@ -106,6 +106,43 @@ GBM_API int gbm_target_hierarchical_normal(gbm_context* ctx, const float* y, con
                                            int64_t groups, float mu_scale, float tau_scale,
                                            gbm_target** out);
 
+/* Many independent posteriors of uneven dimension in one target, for one
+ * NoUTurnSampler over all of them (one set of launches per sampler step for
+ * every member).  Each member is a multivariate normal (loc, L^-1 and
+ * log_normalizer as for gbm_target_mvn) or a non-centred hierarchical normal
+ * (group_y, group_sigma, mu_scale, tau_scale as for
+ * gbm_target_hierarchical_normal; its state dimension is dim + 2), with its
+ * own number of chains.  There is no single reference object for this: it
+ * replaces running one tfp.mcmc.NoUTurnSampler (mcmc/nuts.py:165) per
+ * posterior with per-chain step sizes (nuts.py:237-243 allows [C, 1] step
+ * sizes).  States, gradients and momenta are ragged: member t's chains come
+ * after member t-1's, and chain c's vector has dims[c] float32 elements
+ * starting at element offsets[c] (gbm_target_batch_layout).  The
+ * log-density of every chain is one float64.  Inputs are copied. */
+typedef struct gbm_batch_member {
+  int32_t family;                 /* GBM_FAMILY_MVN or GBM_FAMILY_HIERARCHICAL_NORMAL */
+  int64_t dim;                    /* MVN: state dimension; hierarchical: groups J */
+  int64_t chains;                 /* chains sampling this posterior */
+  const float* loc;               /* MVN [dim] */
+  const float* scale_tril_inv;    /* MVN [dim][dim], lower triangular */
+  double log_normalizer;          /* MVN */
+  const float* group_y;           /* hierarchical [J] */
+  const float* group_sigma;       /* hierarchical [J] */
+  float mu_scale, tau_scale;      /* hierarchical */
+} gbm_batch_member;
+
+GBM_API int gbm_target_batch(gbm_context* ctx, const gbm_batch_member* members, int64_t count,
+                             gbm_target** out);
+/* Ragged layout of a batch target (host arrays of `chains` entries, either
+ * may be NULL): per-chain element offsets and dimensions, the number of
+ * chains and the total number of state elements. */
+GBM_API int gbm_target_batch_layout(const gbm_target* target, int64_t* offsets, int32_t* dims,
+                                    int64_t* chains, int64_t* elements);
+/* Chain-tile width (32 or 64 chains) the construction-time autotuner chose
+ * for multivariate-normal members with dim <= 64, <= 256, <= 1024 and
+ * > 1024 (0: no member in that class). */
+GBM_API int gbm_target_batch_schedule(const gbm_target* target, int32_t chain_tile[4]);
+
 GBM_API int gbm_target_destroy(gbm_target* target);
 GBM_API int gbm_target_dim(const gbm_target* target, int64_t* dim);
 

@@ -117,3 +117,49 @@ class PhiloxDraws:
 
   def tree_uniform(self, c, depth):
     return uniform(self.key, 'tree_uniform', c, depth)
+
+
+def _bits_at(key, kind, idx, depth=0, leaf=0):
+  idx = np.asarray(idx, dtype=np.uint64)
+  z = np.zeros_like(idx)
+  return philox4x32_10(key, (idx, z + _site(kind, depth, leaf), z, z))
+
+
+class OffsetDraws(PhiloxDraws):
+  """Draws of a block of chains that sits inside a larger ragged batch (the
+  engine's many-posterior sampler): chain i of the block is chain chain0 + i
+  of the batch, and its state element d is batch element elem0 + i * D + d.
+  Same streams as PhiloxDraws, addressed by those batch indices."""
+
+  def __init__(self, key, chain0, elem0):
+    super().__init__(key)
+    self.chain0 = int(chain0)
+    self.elem0 = int(elem0)
+
+  def _chains(self, c):
+    return self.chain0 + np.arange(c, dtype=np.uint64)
+
+  def momentum(self, shape):
+    n = int(np.prod(shape))
+    o0, o1, _, _ = _bits_at(self.key, 'momentum', self.elem0 + np.arange(n, dtype=np.uint64))
+    u1 = ((o0 >> np.uint32(8)).astype(np.float64) + 1.0) * 2.0 ** -24
+    u2 = (o1 >> np.uint32(8)).astype(np.float64) * 2.0 ** -24
+    z = np.sqrt(-2.0 * np.log(u1)) * np.cos(2.0 * np.pi * u2)
+    return z.astype(np.float32).reshape(shape)
+
+  def _uniform(self, kind, c, depth=0, leaf=0):
+    o0, _, _, _ = _bits_at(self.key, kind, self._chains(c), depth, leaf)
+    return ((o0 >> np.uint32(8)).astype(np.float64) * 2.0 ** -24).astype(np.float32)
+
+  def mh_uniform(self, c):
+    return self._uniform('mh_uniform', c)
+
+  def direction(self, c, depth):
+    o0, _, _, _ = _bits_at(self.key, 'direction', self._chains(c), depth, 0)
+    return (o0 >> np.uint32(31)).astype(np.int32)
+
+  def leaf_uniform(self, c, depth, leaf):
+    return self._uniform('leaf_uniform', c, depth, leaf)
+
+  def tree_uniform(self, c, depth):
+    return self._uniform('tree_uniform', c, depth)

@@ -227,6 +227,65 @@ int gbm_target_hierarchical_normal(gbm_context* ctx, const float* y, const float
   });
 }
 
+int gbm_target_batch(gbm_context* ctx, const gbm_batch_member* m, int64_t count,
+                     gbm_target** out) {
+  if (!ctx || !m || !out) return invalid("gbm_target_batch: NULL argument");
+  if (count <= 0 || count > (1 << 20)) return invalid("gbm_target_batch: bad member count");
+  int64_t chains = 0, elems = 0;
+  for (int64_t i = 0; i < count; ++i) {
+    const gbm_batch_member& b = m[i];
+    if (b.chains <= 0 || b.dim <= 0 || b.dim > (1 << 16))
+      return invalid("gbm_target_batch: every member needs chains > 0 and 0 < dim <= 65536");
+    if (b.family == GBM_FAMILY_MVN) {
+      if (!b.loc || !b.scale_tril_inv) return invalid("gbm_target_batch: MVN member needs loc, L^-1");
+    } else if (b.family == GBM_FAMILY_HIERARCHICAL_NORMAL) {
+      if (!b.group_y || !b.group_sigma || !(b.mu_scale > 0.f) || !(b.tau_scale > 0.f))
+        return invalid("gbm_target_batch: hierarchical member needs y, sigma and scales > 0");
+    } else {
+      return invalid("gbm_target_batch: members are MVN or hierarchical-normal");
+    }
+    chains += b.chains;
+    elems += b.chains * (b.family == GBM_FAMILY_MVN ? b.dim : b.dim + 2);
+  }
+  if (chains > (1 << 24) || elems > ((int64_t)1 << 34))
+    return invalid("gbm_target_batch: too many chains or state elements");
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    std::unique_ptr<gbm_target> t(new gbm_target());
+    t->ctx = ctx;
+    t->impl = gbm::make_batch(ctx, m, count);
+    finish_target(ctx, t.get(), out);
+    t.release();
+    return GBM_OK;
+  });
+}
+
+int gbm_target_batch_layout(const gbm_target* t, int64_t* offsets, int32_t* dims,
+                            int64_t* chains, int64_t* elements) {
+  if (!t) return invalid("gbm_target_batch_layout: NULL target");
+  const int64_t C = t->impl->ragged_chains();
+  if (C == 0) return invalid("gbm_target_batch_layout: not a batch target");
+  return guarded([&] {
+    DeviceGuard g(t->ctx->device);
+    if (offsets)
+      GBM_CUDA(cudaMemcpy(offsets, t->impl->ragged_offsets(), sizeof(int64_t) * C,
+                          cudaMemcpyDeviceToHost));
+    if (dims)
+      GBM_CUDA(cudaMemcpy(dims, t->impl->ragged_dims(), sizeof(int32_t) * C,
+                          cudaMemcpyDeviceToHost));
+    if (chains) *chains = C;
+    if (elements) *elements = t->impl->ragged_elements();
+    return GBM_OK;
+  });
+}
+
+int gbm_target_batch_schedule(const gbm_target* t, int32_t chain_tile[4]) {
+  if (!t || !chain_tile) return invalid("gbm_target_batch_schedule: NULL argument");
+  if (!gbm::batch_schedule(t->impl.get(), chain_tile))
+    return invalid("gbm_target_batch_schedule: not a batch target");
+  return GBM_OK;
+}
+
 int gbm_target_destroy(gbm_target* t) {
   if (!t) return GBM_OK;
   return guarded([&] {
@@ -265,6 +324,8 @@ int gbm_target_log_prob_and_grad(gbm_target* t, const float* state, int64_t chai
       t->ws.reserve(need);
     }
     const int n = (int)chains;
+    if (t->impl->ragged_chains() && chains != t->impl->ragged_chains())
+      return invalid("gbm_target_log_prob_and_grad: a batch target evaluates all its chains");
     gbm::set_count(t->count.as<int>(), n, s);
     t->impl->eval(state, (int)t->impl->dim, t->count.as<int>(), n, log_prob, grad,
                   (int)t->impl->dim, t->ws.ptr, s);
@@ -337,6 +398,8 @@ int gbm_nuts_create(gbm_target* target, int64_t max_chains, int32_t max_tree_dep
     return invalid("max_tree_depth must be known statically and >= 1 (engine limit 16)");
   if (max_chains <= 0 || max_chains > (1 << 24)) return invalid("gbm_nuts_create: bad max_chains");
   if (unrolled_leapfrog_steps < 1) return invalid("gbm_nuts_create: unrolled_leapfrog_steps < 1");
+  if (target->impl->ragged_chains() && max_chains != target->impl->ragged_chains())
+    return invalid("gbm_nuts_create: a batch target's sampler runs exactly its chains");
   return guarded([&] {
     DeviceGuard g(target->ctx->device);
     auto* k = new gbm_nuts();
@@ -366,6 +429,7 @@ int gbm_nuts_destroy(gbm_nuts* k) {
     for (auto& ev : k->poll_events)
       if (ev) cudaEventDestroy(ev);
     for (auto& ev : k->prof_events) cudaEventDestroy(ev);
+    gbm::nuts_release_graphs(k);
     delete k;
     return GBM_OK;
   });
@@ -384,6 +448,8 @@ int gbm_nuts_one_step(gbm_nuts* k, int64_t chains, const float* state,
     return invalid("gbm_nuts_one_step: NULL argument");
   if (chains <= 0 || chains > k->max_chains)
     return invalid("gbm_nuts_one_step: chains must be in [1, max_chains]");
+  if (k->dev.ragged && chains != k->max_chains)
+    return invalid("gbm_nuts_one_step: a batch target's sampler steps all its chains");
   return guarded([&] {
     DeviceGuard g(k->target->ctx->device);
     gbm::NutsOutputs out{next_state, next_tlp, next_grads, log_accept_ratio, leapfrogs_taken,

@@ -8,6 +8,8 @@
 
 #include "common.cuh"
 
+struct gbm_batch_member;   // include/gb300_mcmc.h
+
 struct gbm_context {
   int device = 0;
   cudaStream_t stream = nullptr;
@@ -78,6 +80,18 @@ struct Target {
   virtual double bytes(int64_t n) const = 0;
   // Kernels one eval() launches (for launch accounting).
   virtual int launches_per_eval() const = 0;
+  // Ragged batches of posteriors (many targets of different dimension in one
+  // sampler): per-chain element offsets and dimensions on the device, the
+  // number of chains and the sum of their dimensions.  Uniform targets
+  // return nullptr / 0.
+  virtual const int64_t* ragged_offsets() const { return nullptr; }
+  virtual const int* ragged_dims() const { return nullptr; }
+  virtual int64_t ragged_chains() const { return 0; }
+  virtual int64_t ragged_elements() const { return 0; }
+  // Ragged evaluation in place: the chains act_idx[0 .. *act_count) (sorted),
+  // states and gradients at their element offsets, logp indexed by chain.
+  virtual void eval_active(const float* q, const int* act_idx, const int* act_count,
+                           double* logp, float* grad, void* ws, cudaStream_t s) {}
 };
 
 // Fill / release a context (pinned host words, mapped error word).
@@ -101,6 +115,11 @@ std::unique_ptr<Target> make_mvn(gbm_context* ctx, const float* loc, const float
                                  int64_t d, double log_norm);
 std::unique_ptr<Target> make_hier(gbm_context* ctx, const float* y, const float* sigma, int64_t J,
                                   float mu_scale, float tau_scale);
+
+std::unique_ptr<Target> make_batch(gbm_context* ctx, const ::gbm_batch_member* members,
+                                   int64_t count);
+// Chain tiles chosen by the batch autotuner (false: `t` is not a batch).
+bool batch_schedule(const Target* t, int32_t* chain_tile);
 
 std::unique_ptr<Target> make_logreg_simt(gbm_context* ctx, const float* X, int64_t n,
                                          int64_t d, const float* y, float prior_scale);

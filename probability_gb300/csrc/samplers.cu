@@ -38,6 +38,24 @@ __device__ __forceinline__ float eps_of(const float* eps, int per_chain, int c) 
   return per_chain ? eps[c] : eps[0];
 }
 
+// Layout helpers (uniform or ragged, see NutsDev).
+__device__ __forceinline__ size_t voff(const NutsDev& w, int c) {
+  return w.ragged ? (size_t)w.coff[c] : (size_t)c * w.D;
+}
+__device__ __forceinline__ int vdim(const NutsDev& w, int c) {
+  return w.ragged ? w.cdim[c] : w.D;
+}
+// Start of U-turn slot i of chain c.
+__device__ __forceinline__ size_t soff(const NutsDev& w, int c, int i) {
+  return w.ragged ? (size_t)w.coff[c] * w.slots + (size_t)i * w.cdim[c]
+                  : ((size_t)c * w.slots + i) * w.D;
+}
+// Start of chain c (at batch position j) in the gradient batch qw / gw.
+__device__ __forceinline__ size_t boff(const NutsDev& w, int c, int j) {
+  return w.ragged ? (size_t)w.coff[c] : (size_t)j * w.D;
+}
+__device__ __forceinline__ int lwi(const NutsDev& w, int c, int j) { return w.ragged ? c : j; }
+
 // --------------------------------------------------------------------------
 // Active-chain compaction: idx[0..count) = chains with (flags & bit), sorted.
 // --------------------------------------------------------------------------
@@ -83,6 +101,7 @@ cudaStream_t& alloc_stream() {
 }
 
 __global__ void set_count_kernel(int* count, int n) { *count = n; }
+__global__ void set_key_kernel(uint2* keyp, uint2 key) { *keyp = key; }
 
 void set_count(int* count, int n, cudaStream_t s) {
   set_count_kernel<<<1, 1, 0, s>>>(count, n);
@@ -102,8 +121,8 @@ __global__ void nuts_init_kernel(NutsDev w, const float* __restrict__ q,
                                  const float* __restrict__ eps_in, int eps_per_chain, uint2 key) {
   const int c = warp_id(), lane = threadIdx.x & 31;
   if (c >= w.C) return;
-  const int D = w.D;
-  const size_t o = (size_t)c * D;
+  const int D = vdim(w, c);
+  const size_t o = voff(w, c);
   const uint32_t site = draw_site(kDrawMomentum, 0, 0);
   double kin = 0.0;
   for (int d = lane; d < D; d += 32) {
@@ -148,9 +167,11 @@ __global__ void nuts_depth_begin_kernel(NutsDev w, uint2 key, int depth) {
 }
 
 __global__ void nuts_zero_cumsum_kernel(NutsDev w) {
-  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t n = (size_t)w.C * w.D;
-  if (i < n && (w.flags[i / w.D] & kSubCont)) w.cumsum[i] = 0.f;
+  const int c = warp_id(), lane = threadIdx.x & 31;
+  if (c >= w.C || !(w.flags[c] & kSubCont)) return;
+  const size_t o = voff(w, c);
+  const int D = vdim(w, c);
+  for (int d = lane; d < D; d += 32) w.cumsum[o + d] = 0.f;
 }
 
 // Half kick + drift for the active chains; writes the dense batch qw.
@@ -162,11 +183,12 @@ __global__ void nuts_leaf_pre_kernel(NutsDev w) {
   const int side = (w.flags[c] & kForward) ? 1 : 0;
   const float e = (side ? 1.f : -1.f) * w.eps[c];
   const float he = 0.5f * e;
-  const size_t o = (size_t)c * w.D, oj = (size_t)j * w.D;
+  const size_t o = voff(w, c), oj = boff(w, c, j);
+  const int D = vdim(w, c);
   float* P = w.end_p[side];
   float* Q = w.end_q[side];
   const float* G = w.end_g[side];
-  for (int d = lane; d < w.D; d += 32) {
+  for (int d = lane; d < D; d += 32) {
     const float ph = P[o + d] + he * G[o + d];
     const float qn = Q[o + d] + e * ph;
     P[o + d] = ph;
@@ -182,8 +204,9 @@ __global__ void nuts_leaf_mid_kernel(NutsDev w) {
   const int c = w.act_idx[j];
   const int side = (w.flags[c] & kForward) ? 1 : 0;
   const float e = (side ? 1.f : -1.f) * w.eps[c];
-  const size_t o = (size_t)c * w.D, oj = (size_t)j * w.D;
-  for (int d = lane; d < w.D; d += 32) {
+  const size_t o = voff(w, c), oj = boff(w, c, j);
+  const int D = vdim(w, c);
+  for (int d = lane; d < D; d += 32) {
     const float ph = w.end_p[side][o + d] + e * w.gw[oj + d];
     const float qn = w.end_q[side][o + d] + e * ph;
     w.end_p[side][o + d] = ph;
@@ -195,17 +218,19 @@ __global__ void nuts_leaf_mid_kernel(NutsDev w) {
 // Final kick, slot bookkeeping, U-turn checks, energy, multinomial leaf
 // sampling: _loop_build_sub_tree (nuts.py:793-946) and
 // has_not_u_turn_at_all_index (nuts.py:949-984).
-__global__ void nuts_leaf_post_kernel(NutsDev w, uint2 key, int depth, int leaf, int wslot,
-                                      int r0, int r1, double max_energy_diff) {
+__global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp, int depth,
+                                      int leaf, int wslot, int r0, int r1,
+                                      double max_energy_diff) {
   const int j = warp_id(), lane = threadIdx.x & 31;
   if (j >= *w.act_count) return;
+  const uint2 key = *keyp;
   const int c = w.act_idx[j];
-  const int D = w.D;
+  const int D = vdim(w, c);
   const uint8_t f = w.flags[c];
   const int side = (f & kForward) ? 1 : 0;
   const float e = (side ? 1.f : -1.f) * w.eps[c];
   const float he = 0.5f * e;
-  const size_t o = (size_t)c * D, oj = (size_t)j * D;
+  const size_t o = voff(w, c), oj = boff(w, c, j);
   float* P = w.end_p[side];
   float* Gs = w.end_g[side];
   double kin = 0.0;
@@ -218,7 +243,7 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, uint2 key, int depth, int leaf,
     const float cs = csp + p2;                          // nuts.py:827-828
     w.cumsum[o + d] = cs;
     if (wslot >= 0) {                                   // nuts.py:857-869
-      const size_t so = ((size_t)c * w.slots + wslot) * D + d;
+      const size_t so = soff(w, c, wslot) + d;
       w.slot_p[so] = p2;
       w.slot_cs[so] = csp;
     }
@@ -231,7 +256,7 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, uint2 key, int depth, int leaf,
   bool no_uturn = true;
   for (int i = r0; i < r1; ++i) {
     double dl = 0.0, dr = 0.0;
-    const size_t so = ((size_t)c * w.slots + i) * D;
+    const size_t so = soff(w, c, i);
     for (int d = lane; d < D; d += 32) {
       const float diff = w.cumsum[o + d] - w.slot_cs[so + d];
       dl += (double)diff * (double)w.slot_p[so + d];
@@ -241,7 +266,7 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, uint2 key, int depth, int leaf,
     dr = warp_sum(dr);
     no_uturn = no_uturn && (dl >= 0.0) && (dr >= 0.0);
   }
-  const double l2 = w.lw[j];
+  const double l2 = w.lw[lwi(w, c, j)];
   double energy = l2 - 0.5 * kin;                         // nuts.py:871-876
   if (isnan(energy)) energy = -INFINITY;
   const double de = energy - w.e0[c];
@@ -277,8 +302,8 @@ __global__ void nuts_depth_end_kernel(NutsDev w, uint2 key, int depth) {
   if (c >= w.C) return;
   const uint8_t f = w.flags[c];
   if (!(f & kCont)) return;
-  const int D = w.D;
-  const size_t o = (size_t)c * D;
+  const int D = vdim(w, c);
+  const size_t o = voff(w, c);
   const bool sub_cont = f & kSubCont;
   const double tree_w = sub_cont ? w.sub_w[c] : -INFINITY;
   const double cw = w.cand_w[c];
@@ -318,8 +343,9 @@ __global__ void nuts_depth_end_kernel(NutsDev w, uint2 key, int depth) {
 __global__ void nuts_finalize_kernel(NutsDev w, NutsOutputs out, int unrolled) {
   const int c = warp_id(), lane = threadIdx.x & 31;
   if (c >= w.C) return;
-  const size_t o = (size_t)c * w.D;
-  for (int d = lane; d < w.D; d += 32) {
+  const size_t o = voff(w, c);
+  const int D = vdim(w, c);
+  for (int d = lane; d < D; d += 32) {
     out.state[o + d] = w.cand_q[o + d];
     out.grads[o + d] = w.cand_g[o + d];
   }
@@ -527,13 +553,17 @@ void nuts_instructions(int depth, std::vector<int>* write, std::vector<int>* lo,
 void nuts_setup(gbm_nuts* k) {
   int slots = 0;
   nuts_instructions(k->max_tree_depth, &k->write_instr, &k->read_lo, &k->read_hi, &slots);
-  const int64_t C = k->max_chains, D = k->target->impl->dim;
+  const Target* t = k->target->impl.get();
+  const int64_t C = k->max_chains, D = t->dim;
   NutsDev& w = k->dev;
   w.C = (int)C;
   w.D = (int)D;
   w.slots = slots;
+  w.ragged = t->ragged_offsets() != nullptr;
+  w.coff = t->ragged_offsets();
+  w.cdim = t->ragged_dims();
   // Carve one allocation: float vectors, slot memory, doubles, ints, bytes.
-  const size_t vec = (size_t)C * D;
+  const size_t vec = w.ragged ? (size_t)t->ragged_elements() : (size_t)C * D;
   const size_t n_float_vecs = 6 + 6 + 2;   // ends(6), cand/sub/mom/cumsum(6), qw/gw(2)
   size_t bytes = 0;
   auto take = [&](size_t b) { size_t at = bytes; bytes += (b + 255) / 256 * 256; return at; };
@@ -569,11 +599,24 @@ void nuts_setup(gbm_nuts* k) {
   GBM_CUDA(cudaMemsetAsync(base, 0, bytes, k->ctx->stream));
   k->target_ws.reserve(k->target->impl->workspace_bytes(C));
   for (auto& ev : k->poll_events) GBM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+  k->key_dev.reserve(sizeof(uint2));
+  // Graph replay needs a stream that can be captured (not the legacy one).
+  k->use_graphs = w.ragged && k->ctx->stream != nullptr;
 }
 
-static void nuts_eval(gbm_nuts* k, cudaStream_t s) {
+void nuts_release_graphs(gbm_nuts* k) {
+  for (auto& g : k->graphs) cudaGraphExecDestroy(g.second);
+  k->graphs.clear();
+}
+
+static void nuts_eval(gbm_nuts* k, cudaStream_t s, bool capturing = false) {
   const NutsDev& w = k->dev;
-  if (k->profiling) {
+  if (w.ragged) {
+    k->target->impl->eval_active(w.qw, w.act_idx, w.act_count, w.lw, w.gw, k->target_ws.ptr, s);
+    if (!capturing) k->prof_launches += k->target->impl->launches_per_eval();
+    return;
+  }
+  if (k->profiling && !capturing) {
     if (k->prof_used + 2 > k->prof_events.size()) {
       cudaEvent_t a, b;
       GBM_CUDA(cudaEventCreate(&a));
@@ -585,7 +628,7 @@ static void nuts_eval(gbm_nuts* k, cudaStream_t s) {
   }
   k->target->impl->eval(w.qw, w.D, w.act_count, w.C, w.lw, w.gw, w.D, k->target_ws.ptr, s);
   k->prof_launches += k->target->impl->launches_per_eval();
-  if (k->profiling) {
+  if (k->profiling && !capturing) {
     GBM_CUDA(cudaEventRecord(k->prof_events[k->prof_used + 1], s));
     k->prof_used += 2;
     ++k->prof_evals;
@@ -610,10 +653,27 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
   w.C = (int)chains;
   int* host_flags = ctx->host_flags;
   const int wb = warp_blocks(chains), tb = 256;
+  const uint2* keyp = k->key_dev.as<uint2>();
+  set_key_kernel<<<1, 1, 0, s>>>(k->key_dev.as<uint2>(), key);
   nuts_init_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, q, l, g, eps, eps_per_chain, key);
   GBM_CUDA(cudaGetLastError());
   k->last_leaf_iterations = 0;
-  const size_t vec = (size_t)chains * w.D;
+  // One leaf: half kick + drift, gradient, final kick and tree bookkeeping,
+  // then the next active list.
+  auto leaf_step = [&](int depth, int leaf, bool capturing) {
+    nuts_leaf_pre_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w);
+    nuts_eval(k, s, capturing);
+    for (int u = 1; u < k->unrolled_leapfrog_steps; ++u) {
+      nuts_leaf_mid_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w);
+      nuts_eval(k, s, capturing);
+    }
+    nuts_leaf_post_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(
+        w, keyp, depth, leaf, k->write_instr[leaf], k->read_lo[leaf], k->read_hi[leaf],
+        k->max_energy_diff);
+    GBM_CUDA(cudaGetLastError());
+    build_active(w, kSubCont, s);
+    if (!capturing) k->prof_launches += 3 + (k->unrolled_leapfrog_steps - 1);
+  };
   for (int depth = 0; depth < k->max_tree_depth; ++depth) {
     if (depth > 0) {
       GBM_CUDA(cudaMemcpyAsync(host_flags, w.any_cont, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -623,7 +683,7 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
       if (host_flags[0] == 0) break;
     }
     nuts_depth_begin_kernel<<<(int)((chains + tb - 1) / tb), tb, 0, s>>>(w, key, depth);
-    nuts_zero_cumsum_kernel<<<(int)((vec + tb - 1) / tb), tb, 0, s>>>(w);
+    nuts_zero_cumsum_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w);
     build_active(w, kSubCont, s);
     const int leaves = 1 << depth;
     const int batch = 8;
@@ -643,19 +703,32 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
           if (host_flags[1 + prev] == 0) break;
         }
       }
-      nuts_leaf_pre_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w);
-      nuts_eval(k, s);
-      for (int u = 1; u < k->unrolled_leapfrog_steps; ++u) {
-        nuts_leaf_mid_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w);
-        nuts_eval(k, s);
+      if (k->use_graphs && leaf % batch == 0) {
+        // The next `nl` leaves as one graph launch (leaves whose subtree has
+        // ended cost a launch of idle warps only).
+        const int nl = std::min(batch, leaves - leaf);
+        const int gkey = depth * 4096 + leaf;
+        auto it = k->graphs.find(gkey);
+        if (it == k->graphs.end()) {
+          cudaGraph_t graph;
+          GBM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+          for (int l = leaf; l < leaf + nl; ++l) leaf_step(depth, l, true);
+          GBM_CUDA(cudaStreamEndCapture(s, &graph));
+          cudaGraphExec_t exec;
+          GBM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+          GBM_CUDA(cudaGraphDestroy(graph));
+          it = k->graphs.emplace(gkey, exec).first;
+        }
+        GBM_CUDA(cudaGraphLaunch(it->second, s));
+        ++k->graph_launches;
+        k->prof_launches += (int64_t)nl * (3 + k->unrolled_leapfrog_steps * (
+            k->target->impl->launches_per_eval() + 1) - 1);
+        k->last_leaf_iterations += nl;
+        leaf += nl - 1;
+        continue;
       }
-      nuts_leaf_post_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(
-          w, key, depth, leaf, k->write_instr[leaf], k->read_lo[leaf], k->read_hi[leaf],
-          k->max_energy_diff);
-      GBM_CUDA(cudaGetLastError());
-      build_active(w, kSubCont, s);
+      leaf_step(depth, leaf, false);
       ++k->last_leaf_iterations;
-      k->prof_launches += 3 + (k->unrolled_leapfrog_steps - 1);
     }
     nuts_depth_end_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, key, depth);
     GBM_CUDA(cudaGetLastError());

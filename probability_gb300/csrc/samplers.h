@@ -2,6 +2,7 @@
 #pragma once
 #include <stdint.h>
 
+#include <map>
 #include <vector>
 
 #include "engine.h"
@@ -19,8 +20,16 @@ enum ChainFlag : uint8_t {
 };
 
 // Device pointers of the NUTS workspace (passed to kernels by value).
+// Uniform layout: chain c's D-vector starts at c * D.  Ragged layout (many
+// posteriors of different dimension in one sampler): chain c's vector has
+// cdim[c] elements starting at coff[c], its U-turn slots start at
+// coff[c] * slots, and the gradient batch is evaluated in place (qw, gw at
+// coff[c], lw[c]) instead of compacted.
 struct NutsDev {
   int C, D, slots;
+  int ragged;
+  const int64_t* coff;      // [C] element offsets (ragged)
+  const int* cdim;          // [C] dimensions (ragged)
   float* end_q[2];
   float* end_p[2];
   float* end_g[2];
@@ -128,6 +137,14 @@ struct gbm_nuts {
   gbm::DeviceBuffer loop_mem;   // chain-loop ping-pong and result buffers
   gbm::NutsDev dev{};
   cudaEvent_t poll_events[4] = {nullptr, nullptr, nullptr, nullptr};
+  // CUDA-graph replay of batches of leaves (ragged batches on a non-default
+  // stream): one executable graph per (depth, first leaf), captured on first
+  // use; the transition key is read from key_dev so graphs are reused by
+  // every transition.
+  bool use_graphs = false;
+  std::map<int, cudaGraphExec_t> graphs;
+  gbm::DeviceBuffer key_dev;   // uint2
+  int64_t graph_launches = 0;
   // Counters for the last transition (host-visible after one_step returns).
   int64_t last_leaf_iterations = 0;
   // Optional profiling: CUDA events bracket every batched target evaluation.
@@ -141,6 +158,7 @@ struct gbm_nuts {
 
 namespace gbm {
 void nuts_profile_flush(gbm_nuts* k);  // stream must be synchronized
+void nuts_release_graphs(gbm_nuts* k);
 }  // namespace gbm
 
 struct gbm_hmc {

@@ -167,6 +167,7 @@ void run_job(gbm_context* ctx, Job* job) {
   for (auto& ev : k.poll_events)
     if (ev) cudaEventDestroy(ev);
   for (auto& ev : k.prof_events) cudaEventDestroy(ev);
+  nuts_release_graphs(&k);
 }
 
 void worker_main(gbm_server* srv) {

@@ -129,6 +129,8 @@ class MultivariateNormalTriL(Target):
                   'gbm_target_mvn')
     self._handle = h
     self._ctx = ctx
+    # Device parameters, reused when the target joins a TargetBatch.
+    self._loc_t, self._linv_t, self._log_norm, self.event_dim = loc_t, linv_t, float(log_norm), d
 
 
 class NonCentredHierarchicalNormal(Target):
@@ -148,6 +150,9 @@ class NonCentredHierarchicalNormal(Target):
         float(tau_scale), ctypes.byref(h)), 'gbm_target_hierarchical_normal')
     self._handle = h
     self._ctx = ctx
+    self._y_t, self._s_t = y_t, s_t
+    self.mu_scale, self.tau_scale = float(mu_scale), float(tau_scale)
+    self.event_dim = self.groups + 2
 
 
 def resolve(target_log_prob_fn):
