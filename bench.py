@@ -45,6 +45,13 @@ WORKLOADS['nuts_logreg_1e6x512_bf16'] = dict(n=1000000, d=512, chains=4096, dept
                                              precision_report=10000)
 WORKLOADS['hmc_logreg_1000x25'] = dict(n=1000, d=25, chains=64, seed=0, feature_scale=1.0,
                                        step0=0.03, leapfrogs=10, burnin=500, precision='fp32')
+# Batched uneven posteriors: 128 multivariate normals, D ~ log-U[8, 2048],
+# covariance ~ Wishart(D + 2, I / D); 128 non-centred hierarchical normals,
+# J ~ U{8..512}, mu ~ N(0, 5^2), tau ~ HalfCauchy(5), sigma_j ~ U(5, 20),
+# y_j ~ N(mu + tau z_j, sigma_j^2); 32-512 chains each; NUTS depth 10; one
+# step size per posterior from dual averaging during the warm-in.
+WORKLOADS['nuts_batch_256'] = dict(mvn=128, hier=128, d_range=(8, 2048), j_range=(8, 512),
+                                   chains=(32, 512), depth=10, seed=3, target_accept=0.8)
 # Serving: a Poisson(200/s) stream of DA(NUTS) logistic-regression jobs, each
 # with N ~ log-U[1e3, 2e5] rows, D ~ log-U[10, 1000] features (BF16 X, N(0,
 # 1/D), intercept column), 16-256 chains, 500-5000 draws after 300
@@ -579,6 +586,138 @@ def run_engine(args, w):
     dist.destroy_process_group()
 
 
+def make_batch_members(w):
+  """The 256 posteriors (seeded numpy default_rng)."""
+  rng = np.random.default_rng(w['seed'])
+  spec = []
+  for _ in range(w['mvn']):
+    d = int(np.exp(rng.uniform(np.log(w['d_range'][0]), np.log(w['d_range'][1]))))
+    A = rng.standard_normal((d, d + 2)) / np.sqrt(d)       # Wishart(d + 2, I / d)
+    L = np.linalg.cholesky(A @ A.T)
+    spec.append(('mvn', rng.normal(size=d), L, int(rng.integers(w['chains'][0],
+                                                              w['chains'][1] + 1))))
+  for _ in range(w['hier']):
+    J = int(rng.integers(w['j_range'][0], w['j_range'][1] + 1))
+    mu = rng.normal() * 5.0
+    tau = abs(5.0 * np.tan(np.pi * (rng.uniform() - 0.5)))   # HalfCauchy(5)
+    sigma = rng.uniform(5, 20, J)
+    y = mu + tau * rng.normal(size=J) + sigma * rng.normal(size=J)
+    spec.append(('hier', y, sigma, int(rng.integers(w['chains'][0], w['chains'][1] + 1))))
+  return spec
+
+
+def run_batch(args, w):
+  """256 uneven posteriors in one BatchedNoUTurnSampler."""
+  import ctypes
+  import torch
+  import probability_gb300 as pg
+  from probability_gb300 import _native
+  from probability_gb300.batch import MemberDualAveraging
+  world, rank, local = dist_setup(args)
+  if rank != 0:
+    return
+  dev = torch.device('cuda', local)
+  torch.cuda.set_device(dev)
+  t_setup = time.perf_counter()
+  spec = make_batch_members(w)
+  members = []
+  for s in spec:
+    if s[0] == 'mvn':
+      members.append((pg.MultivariateNormalTriL(s[1], s[2]), s[3]))
+    else:
+      members.append((pg.NonCentredHierarchicalNormal(s[1], s[2]), s[3]))
+  batch = pg.TargetBatch(members)
+  rng = np.random.default_rng(w['seed'] + 1)
+  q = batch.pack([torch.from_numpy((rng.normal(size=(c, t.event_dim)) * 0.5)
+                                   .astype(np.float32)) for t, c in members]).to(dev)
+  setup_s = time.perf_counter() - t_setup
+  da = MemberDualAveraging(batch, 0.1, args.warm_in, target_accept_prob=w['target_accept'])
+  k = pg.BatchedNoUTurnSampler(batch, da.step_size, max_tree_depth=w['depth'])
+  kr = k.bootstrap_results(q)
+  t = 0
+  for _ in range(args.warm_in):            # per-posterior dual averaging
+    q, kr = k.one_step(q, kr._replace(step_size=batch.per_chain(da.step_size)),
+                       seed=pg._util.step_key((w['seed'], 0), t))
+    da.update(kr.log_accept_ratio)
+    t += 1
+  eps = batch.per_chain(da.step_size)
+  kr = kr._replace(step_size=eps)
+  for _ in range(args.warmup):
+    q, kr = k.one_step(q, kr, seed=pg._util.step_key((w['seed'], 0), t))
+    t += 1
+  torch.cuda.synchronize()
+  ms0, ev0, la0 = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+  _native.lib().gbm_nuts_read_profile(k._handle, ctypes.byref(ms0), ctypes.byref(ev0),
+                                      ctypes.byref(la0))
+  flops_chain = torch.as_tensor(
+      [2.0 * tt.event_dim ** 2 if isinstance(tt, pg.MultivariateNormalTriL)
+       else 10.0 * tt.groups for tt, c in members for _ in range(c)], dtype=torch.float64,
+      device=dev)
+  l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+  clocks = ClockSampler(local)
+  clocks.start()
+  lf_total = torch.zeros((), dtype=torch.int64, device=dev)
+  flops = torch.zeros((), dtype=torch.float64, device=dev)
+  draws, step_ms, leaves = [], 0.0, 0
+  torch.cuda.synchronize()
+  for _ in range(args.steps):
+    l2_flush.zero_()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(batch.stream)
+    q, kr = k.one_step(q, kr, seed=pg._util.step_key((w['seed'], 0), t))
+    e1.record(batch.stream)
+    t += 1
+    leaves += k.last_leaf_iterations
+    lf_total += kr.leapfrogs_taken.sum()
+    flops += (kr.leapfrogs_taken.to(torch.float64) * flops_chain).sum()
+    draws.append(q)
+    e1.synchronize()
+    step_ms += e0.elapsed_time(e1)
+  torch.cuda.synchronize()
+  clk = clocks.stop()
+  ms, ev, la = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+  _native.lib().gbm_nuts_read_profile(k._handle, ctypes.byref(ms), ctypes.byref(ev),
+                                      ctypes.byref(la))
+  secs = step_ms / 1000.0
+  grad_evals = int(lf_total.item())
+  ess_sum = None
+  if args.steps >= 20:
+    D = torch.stack(draws)                  # [steps, elements]
+    ess_sum = 0.0
+    for m in range(len(members)):
+      e0_, n = int(batch.elem_begin[m]), batch.member_chains[m] * batch.member_dims[m]
+      x = D[:, e0_:e0_ + n].view(args.steps, batch.member_chains[m], batch.member_dims[m])
+      ess = pg.mcmc.effective_sample_size(x, filter_beyond_positive_pairs=True,
+                                          cross_chain_dims=1)
+      ess_sum += float(ess.min().item())
+  achieved = float(flops.item()) / secs / 1e12
+  fp32_peak = 2 * 128 * 152 * 2.07e9 / 1e12     # FMA lanes x 2 flop x SMs x max clock
+  line = {
+      'metric': 'grad-evals/s over 256 uneven posteriors in one sampler (sum of min-ESS/s beside)',
+      'value': grad_evals / secs, 'unit': 'grad-evals/s', 'n_gpus': 1, 'steps': args.steps,
+      'warmup': args.warmup, 'ms_per_step': step_ms / args.steps, 'higher_is_better': True,
+      'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32 (f64 energies)',
+      'data': 'synthetic (seeded numpy default_rng(%d))' % w['seed'],
+      'config': {'workload': args.workload, 'posteriors': len(members),
+                 'mvn_dims': [int(tt.event_dim) for tt, _ in members[:w['mvn']]],
+                 'chains_total': batch.chains, 'state_elements': batch.elements,
+                 'max_tree_depth': w['depth'], 'warm_in_transitions': args.warm_in,
+                 'step_size': 'one per posterior, dual averaging (target %.2f) in the warm-in'
+                              % w['target_accept'],
+                 'chain_tile_schedule': batch.schedule(),
+                 'l2': 'flushed between timed steps (256 MB write outside the step events)'},
+      'sum_min_ess_per_s': (ess_sum / secs) if ess_sum is not None else None,
+      'leaves_per_step': leaves / args.steps,
+      'roofline': {'bound': 'fp32', 'achieved': achieved, 'peak': fp32_peak, 'unit': 'TFLOP/s',
+                   'frac': achieved / fp32_peak, 'traffic': None,
+                   'kernel': 'batch_phase_kernel (whole sampler step timed)',
+                   'peak_source': 'nominal FP32 FMA rate at the maximum SM clock'},
+      'setup_s': setup_s, 'gpu_launches': int(la.value), 'clocks': clk,
+  }
+  print(json.dumps(line), flush=True)
+
+
 def run_serving(args, w):
   """Replay the head of a Poisson request stream through the job server and
   report latency percentiles, aggregate min-ESS/s and device throughput."""
@@ -698,6 +837,8 @@ def main():
     run_hmc(args, w)
   elif args.workload.startswith('serve_'):
     run_serving(args, w)
+  elif args.workload.startswith('nuts_batch'):
+    run_batch(args, w)
   else:
     run_engine(args, w)
 

@@ -126,8 +126,9 @@ class TargetBatch(targets.Target):
 
   def per_chain(self, per_member_values, dtype=torch.float32):
     """One value per member -> one per chain."""
-    v = torch.as_tensor(per_member_values, dtype=dtype)
-    return torch.repeat_interleave(v, torch.as_tensor(self.member_chains)).to(_util.device())
+    dev = _util.device()
+    v = torch.as_tensor(per_member_values, dtype=dtype).to(dev)
+    return torch.repeat_interleave(v, torch.as_tensor(self.member_chains, device=dev))
 
   def _enter(self):
     self.stream.wait_stream(torch.cuda.current_stream(self.stream.device))
