@@ -361,10 +361,10 @@ def run_engine(args, w):
   import probability_gb300 as pg
   from probability_gb300 import _native
 
+  from probability_gb300 import replicas
   X, y, init = make_data(w)
-  if world > 1:  # independent replicas: per-rank init state
-    init = (np.random.default_rng(w['seed'] + 100 * rank).normal(size=init.shape) * 0.1
-            ).astype(np.float32)
+  if world > 1:  # independent replicas: per-rank init state and key
+    init = replicas.replica_init(init.shape, w['seed'], rank)
   X_engine = engine_features(X, w)
   target = pg.LogisticRegression(X_engine, y, precision=args.precision or w['precision'])
   nuts = pg.mcmc.NoUTurnSampler(target, step_size=w['step0'], max_tree_depth=w['depth'])
@@ -374,7 +374,7 @@ def run_engine(args, w):
   dev = torch.device('cuda', local)
   state = torch.from_numpy(init).to(dev)
   kr = kernel.bootstrap_results(state)
-  seed = (w['seed'], rank)
+  seed = replicas.replica_key((w['seed'], 0), rank) if world > 1 else (w['seed'], 0)
   t = 0
 
   def step(state, kr, t):
@@ -425,13 +425,8 @@ def run_engine(args, w):
   _native.lib().gbm_nuts_set_profiling(nuts._handle, 0)
   grad_evals = int(lf_total.item())
   secs = step_ms / 1000.0
-  if dist is not None:
-    tt = torch.tensor([secs], device=dev)
-    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-    secs = float(tt.item())
-    ge = torch.tensor([grad_evals], device=dev, dtype=torch.int64)
-    dist.all_reduce(ge)
-    grad_evals = int(ge.item())
+  local_evals = grad_evals
+  secs, grad_evals = replicas.combine_throughput(secs, grad_evals)   # max time, total work
   value = grad_evals / secs
   draws_t = torch.stack(draws)
   min_ess_per_s = None
@@ -442,7 +437,7 @@ def run_engine(args, w):
 
   # ---- roofline of the dominant kernel (batched gradient) ----
   flops_per_grad, bytes_per_batch = target.cost(1)
-  alg_flops = flops_per_grad * (grad_evals if dist is None else int(lf_total.item()))
+  alg_flops = flops_per_grad * local_evals
   peaks, peak_src = read_peaks()
   eval_s = eval_ms.value / 1000.0
   achieved_tflops = alg_flops / eval_s / 1e12 if eval_s > 0 else None
