@@ -234,6 +234,11 @@ GBM_API int gbm_nuts_last_leaf_iterations(const gbm_nuts* kernel, int64_t* out);
  * device time of those evaluations (ms), their count, and the number of
  * kernels this handle launched (targets' kernels included), then resets. */
 GBM_API int gbm_nuts_set_profiling(gbm_nuts* kernel, int enable);
+/* CUDA-graph replay of the per-leaf launch sequence (on by default; steps
+ * taken while profiling is on always launch leaf by leaf).  Replay gives the
+ * same bits as per-leaf launches.  No reference counterpart: tfp.mcmc runs
+ * under tf.function/XLA, which this replaces. */
+GBM_API int gbm_nuts_set_graphs(gbm_nuts* kernel, int enable);
 GBM_API int gbm_nuts_read_profile(gbm_nuts* kernel, double* eval_ms, int64_t* evals,
                                   int64_t* kernel_launches);
 

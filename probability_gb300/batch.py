@@ -11,8 +11,7 @@ vector occupies ``offsets[c] : offsets[c] + dims[c]``; ``pack`` and
 
 Every sampler step launches the same kernels whatever the number of members:
 the per-leaf gradient is two persistent launches over a device-built tile
-list, and batches of leaves are replayed as CUDA graphs (the batch runs on
-its own stream).  The chain-tile width of each size class of D is picked by
+list, and batches of leaves are replayed as CUDA graphs.  The chain-tile width of each size class of D is picked by
 timing at construction (``schedule``).
 """
 import ctypes
@@ -61,8 +60,7 @@ class TargetBatch(targets.Target):
 
   def __init__(self, members, stream=None):
     dev = _util.device()
-    # The batch's own stream: CUDA graphs need a capturable (non-legacy)
-    # stream; on the legacy default stream the sampler launches leaf by leaf.
+    # The batch's own stream (work of the batch is ordered on it).
     self.stream = torch.cuda.Stream(dev) if stream is None else stream
     self.stream.wait_stream(torch.cuda.current_stream(dev))
     arr = (BatchMember * len(members))()
@@ -155,7 +153,7 @@ class BatchedNoUTurnSampler:
   ``step_size`` is one value per member (or per chain)."""
 
   def __init__(self, batch, step_size, max_tree_depth=10, max_energy_diff=1000.,
-               unrolled_leapfrog_steps=1):
+               unrolled_leapfrog_steps=1, use_graphs=True):
     if not isinstance(batch, TargetBatch):
       raise TypeError('BatchedNoUTurnSampler samples a TargetBatch')
     self.batch = batch
@@ -166,6 +164,8 @@ class BatchedNoUTurnSampler:
         batch._handle, batch.chains, self.max_tree_depth, float(max_energy_diff),
         int(unrolled_leapfrog_steps), ctypes.byref(h)), 'gbm_nuts_create')
     self._handle = h
+    _native.check(_native.lib().gbm_nuts_set_graphs(h, int(bool(use_graphs))),
+                  'gbm_nuts_set_graphs')
     self.last_leaf_iterations = 0
 
   def __del__(self):

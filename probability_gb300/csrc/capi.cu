@@ -543,6 +543,12 @@ int gbm_nuts_set_profiling(gbm_nuts* k, int enable) {
   return GBM_OK;
 }
 
+int gbm_nuts_set_graphs(gbm_nuts* k, int enable) {
+  if (!k) return invalid("gbm_nuts_set_graphs: NULL argument");
+  k->use_graphs = enable != 0;
+  return GBM_OK;
+}
+
 int gbm_nuts_read_profile(gbm_nuts* k, double* eval_ms, int64_t* evals, int64_t* launches) {
   if (!k || !eval_ms || !evals || !launches) return invalid("gbm_nuts_read_profile: NULL argument");
   return guarded([&] {

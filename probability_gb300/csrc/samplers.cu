@@ -25,6 +25,7 @@
 namespace gbm {
 
 constexpr int kWarpsPerBlock = 8;
+constexpr int kMaxSlots = 16;   // U-turn slots: max_tree_depth <= 16
 
 static inline int warp_blocks(int64_t n) {
   return (int)((n + kWarpsPerBlock - 1) / kWarpsPerBlock);
@@ -252,19 +253,36 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp,
   kin = warp_sum(kin);
   __syncwarp();
   // Within-subtree U-turn over the read range (reads never hit wslot: a leaf
-  // that ends subtrees writes only the dummy slot, which is skipped).
+  // that ends subtrees writes only the dummy slot, which is skipped).  Every
+  // slot's two dot products are accumulated per lane first and then reduced
+  // across the warp together, so the shuffle latencies overlap.
   bool no_uturn = true;
-  for (int i = r0; i < r1; ++i) {
-    double dl = 0.0, dr = 0.0;
-    const size_t so = soff(w, c, i);
+  const int ns = r1 - r0;
+  if (ns > 0) {
+    double dot[2 * kMaxSlots];
+#pragma unroll
+    for (int k = 0; k < 2 * kMaxSlots; ++k) dot[k] = 0.0;
     for (int d = lane; d < D; d += 32) {
-      const float diff = w.cumsum[o + d] - w.slot_cs[so + d];
-      dl += (double)diff * (double)w.slot_p[so + d];
-      dr += (double)diff * (double)P[o + d];
+      const float cs = w.cumsum[o + d], pd = P[o + d];
+#pragma unroll
+      for (int k = 0; k < kMaxSlots; ++k) {
+        if (k < ns) {
+          const size_t so = soff(w, c, r0 + k) + d;
+          const float diff = cs - w.slot_cs[so];
+          dot[2 * k] += (double)diff * (double)w.slot_p[so];
+          dot[2 * k + 1] += (double)diff * (double)pd;
+        }
+      }
     }
-    dl = warp_sum(dl);
-    dr = warp_sum(dr);
-    no_uturn = no_uturn && (dl >= 0.0) && (dr >= 0.0);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+#pragma unroll
+      for (int k = 0; k < 2 * kMaxSlots; ++k)
+        if (k < 2 * ns) dot[k] += __shfl_xor_sync(0xffffffffu, dot[k], off);
+    }
+#pragma unroll
+    for (int k = 0; k < 2 * kMaxSlots; ++k)
+      if (k < 2 * ns) no_uturn = no_uturn && (dot[k] >= 0.0);
   }
   const double l2 = w.lw[lwi(w, c, j)];
   double energy = l2 - 0.5 * kin;                         // nuts.py:871-876
@@ -600,13 +618,18 @@ void nuts_setup(gbm_nuts* k) {
   k->target_ws.reserve(k->target->impl->workspace_bytes(C));
   for (auto& ev : k->poll_events) GBM_CUDA(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
   k->key_dev.reserve(sizeof(uint2));
-  // Graph replay needs a stream that can be captured (not the legacy one).
-  k->use_graphs = w.ragged && k->ctx->stream != nullptr;
+  // Batches of leaves are captured on a private stream (the caller's may be
+  // the legacy default stream, which cannot be captured) and the executable
+  // graphs are launched on the caller's stream.
+  GBM_CUDA(cudaStreamCreateWithFlags(&k->graph_stream, cudaStreamNonBlocking));
+  k->use_graphs = true;
 }
 
 void nuts_release_graphs(gbm_nuts* k) {
   for (auto& g : k->graphs) cudaGraphExecDestroy(g.second);
   k->graphs.clear();
+  if (k->graph_stream) cudaStreamDestroy(k->graph_stream);
+  k->graph_stream = nullptr;
 }
 
 static void nuts_eval(gbm_nuts* k, cudaStream_t s, bool capturing = false) {
@@ -659,21 +682,24 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
   GBM_CUDA(cudaGetLastError());
   k->last_leaf_iterations = 0;
   // One leaf: half kick + drift, gradient, final kick and tree bookkeeping,
-  // then the next active list.
-  auto leaf_step = [&](int depth, int leaf, bool capturing) {
-    nuts_leaf_pre_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w);
-    nuts_eval(k, s, capturing);
+  // then the next active list (on stream ls: the caller's, or the capture
+  // stream while a graph is recorded).
+  auto leaf_step = [&](int depth, int leaf, bool capturing, cudaStream_t ls) {
+    nuts_leaf_pre_kernel<<<wb, 32 * kWarpsPerBlock, 0, ls>>>(w);
+    nuts_eval(k, ls, capturing);
     for (int u = 1; u < k->unrolled_leapfrog_steps; ++u) {
-      nuts_leaf_mid_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w);
-      nuts_eval(k, s, capturing);
+      nuts_leaf_mid_kernel<<<wb, 32 * kWarpsPerBlock, 0, ls>>>(w);
+      nuts_eval(k, ls, capturing);
     }
-    nuts_leaf_post_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(
+    nuts_leaf_post_kernel<<<wb, 32 * kWarpsPerBlock, 0, ls>>>(
         w, keyp, depth, leaf, k->write_instr[leaf], k->read_lo[leaf], k->read_hi[leaf],
         k->max_energy_diff);
     GBM_CUDA(cudaGetLastError());
-    build_active(w, kSubCont, s);
+    build_active(w, kSubCont, ls);
     if (!capturing) k->prof_launches += 3 + (k->unrolled_leapfrog_steps - 1);
   };
+  // Profiled steps time every gradient evaluation with events: leaf by leaf.
+  const bool graphs = k->use_graphs && !k->profiling;
   for (int depth = 0; depth < k->max_tree_depth; ++depth) {
     if (depth > 0) {
       GBM_CUDA(cudaMemcpyAsync(host_flags, w.any_cont, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -703,17 +729,18 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
           if (host_flags[1 + prev] == 0) break;
         }
       }
-      if (k->use_graphs && leaf % batch == 0) {
+      if (graphs && leaf % batch == 0) {
         // The next `nl` leaves as one graph launch (leaves whose subtree has
         // ended cost a launch of idle warps only).
         const int nl = std::min(batch, leaves - leaf);
-        const int gkey = depth * 4096 + leaf;
+        const int64_t gkey = ((int64_t)chains << 32) | ((int64_t)depth << 16) | leaf;
         auto it = k->graphs.find(gkey);
         if (it == k->graphs.end()) {
           cudaGraph_t graph;
-          GBM_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
-          for (int l = leaf; l < leaf + nl; ++l) leaf_step(depth, l, true);
-          GBM_CUDA(cudaStreamEndCapture(s, &graph));
+          cudaStream_t cs = k->graph_stream;
+          GBM_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+          for (int l = leaf; l < leaf + nl; ++l) leaf_step(depth, l, true, cs);
+          GBM_CUDA(cudaStreamEndCapture(cs, &graph));
           cudaGraphExec_t exec;
           GBM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
           GBM_CUDA(cudaGraphDestroy(graph));
@@ -727,7 +754,7 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
         leaf += nl - 1;
         continue;
       }
-      leaf_step(depth, leaf, false);
+      leaf_step(depth, leaf, false, s);
       ++k->last_leaf_iterations;
     }
     nuts_depth_end_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, key, depth);

@@ -142,7 +142,8 @@ struct gbm_nuts {
   // use; the transition key is read from key_dev so graphs are reused by
   // every transition.
   bool use_graphs = false;
-  std::map<int, cudaGraphExec_t> graphs;
+  cudaStream_t graph_stream = nullptr;   // capture stream (graphs launch on the caller's)
+  std::map<int64_t, cudaGraphExec_t> graphs;   // (chains, depth, first leaf)
   gbm::DeviceBuffer key_dev;   // uint2
   int64_t graph_launches = 0;
   // Counters for the last transition (host-visible after one_step returns).

@@ -96,8 +96,8 @@ def test_batched_nuts_transition_matches_oracle_per_member(pg):
 
 
 def test_graph_replay_is_bit_identical_to_per_leaf_launches(pg):
-  """The batch runs on its own stream (graphs); the same transitions on a
-  copy of the sampler driven leaf by leaf must give the same bits."""
+  """Graph replay of batches of leaves and leaf-by-leaf launches give the
+  same bits."""
   rng = np.random.default_rng(2)
   spec, chains = _members(rng, dims_mvn=(6, 40), groups=(10,), chains=(8, 4, 6))
   batch, _, _ = _build(pg, spec, chains)
@@ -109,9 +109,9 @@ def test_graph_replay_is_bit_identical_to_per_leaf_launches(pg):
   for i in range(4):
     q, kr = k.one_step(q, kr, seed=(9, i))
     states.append(q.clone())
-  # Same sampler on a batch living on the legacy default stream: no graphs.
+  # The same sampler launching leaf by leaf (no graphs), on the legacy stream.
   batch2, _, _ = _build(pg, spec, chains, stream=torch.cuda.default_stream())
-  k2 = pg.BatchedNoUTurnSampler(batch2, [0.1, 0.05, 0.1], max_tree_depth=8)
+  k2 = pg.BatchedNoUTurnSampler(batch2, [0.1, 0.05, 0.1], max_tree_depth=8, use_graphs=False)
   kr2 = k2.bootstrap_results(q0)
   q2 = q0
   for i in range(4):
