@@ -125,7 +125,7 @@ __global__ void nuts_init_kernel(NutsDev w, const float* __restrict__ q,
   const int D = vdim(w, c);
   const size_t o = voff(w, c);
   const uint32_t site = draw_site(kDrawMomentum, 0, 0);
-  double kin = 0.0;
+  float kin_l = 0.f;   // this lane's share of |p|^2 (FP32); summed across lanes in FP64
   for (int d = lane; d < D; d += 32) {
     const float p = draw_normal(key, site, (uint32_t)(o + d));
     const float qd = q[o + d], gd = g[o + d];
@@ -134,9 +134,9 @@ __global__ void nuts_init_kernel(NutsDev w, const float* __restrict__ q,
     w.end_g[0][o + d] = gd; w.end_g[1][o + d] = gd;
     w.cand_q[o + d] = qd;   w.cand_g[o + d] = gd;
     w.mom_sum[o + d] = p;
-    kin += (double)p * (double)p;
+    kin_l = fmaf(p, p, kin_l);
   }
-  kin = warp_sum(kin);
+  const double kin = warp_sum((double)kin_l);
   if (lane == 0) {
     const double lc = l[c];
     const double e0 = lc - 0.5 * kin;   // nuts.py:1085-1102 (negative energy)
@@ -234,7 +234,7 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp,
   const size_t o = voff(w, c), oj = boff(w, c, j);
   float* P = w.end_p[side];
   float* Gs = w.end_g[side];
-  double kin = 0.0;
+  float kin_l = 0.f;
   for (int d = lane; d < D; d += 32) {
     const float g2 = w.gw[oj + d];
     const float p2 = (P[o + d] + e * g2) - he * g2;   // leapfrog_integrator.py:345-349,:304-309
@@ -248,20 +248,22 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp,
       w.slot_p[so] = p2;
       w.slot_cs[so] = csp;
     }
-    kin += (double)p2 * (double)p2;
+    kin_l = fmaf(p2, p2, kin_l);
   }
-  kin = warp_sum(kin);
+  const double kin = warp_sum((double)kin_l);
   __syncwarp();
   // Within-subtree U-turn over the read range (reads never hit wslot: a leaf
-  // that ends subtrees writes only the dummy slot, which is skipped).  Every
-  // slot's two dot products are accumulated per lane first and then reduced
-  // across the warp together, so the shuffle latencies overlap.
+  // that ends subtrees writes only the dummy slot, which is skipped).  The
+  // dot products are FP32, the state's type, as in the reference (GB300's
+  // FP64 pipe is narrow); every slot's two products are accumulated per lane
+  // first and then reduced across the warp together, so the shuffle
+  // latencies overlap.
   bool no_uturn = true;
   const int ns = r1 - r0;
   if (ns > 0) {
-    double dot[2 * kMaxSlots];
+    float dot[2 * kMaxSlots];
 #pragma unroll
-    for (int k = 0; k < 2 * kMaxSlots; ++k) dot[k] = 0.0;
+    for (int k = 0; k < 2 * kMaxSlots; ++k) dot[k] = 0.f;
     for (int d = lane; d < D; d += 32) {
       const float cs = w.cumsum[o + d], pd = P[o + d];
 #pragma unroll
@@ -269,8 +271,8 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp,
         if (k < ns) {
           const size_t so = soff(w, c, r0 + k) + d;
           const float diff = cs - w.slot_cs[so];
-          dot[2 * k] += (double)diff * (double)w.slot_p[so];
-          dot[2 * k + 1] += (double)diff * (double)pd;
+          dot[2 * k] = fmaf(diff, w.slot_p[so], dot[2 * k]);
+          dot[2 * k + 1] = fmaf(diff, pd, dot[2 * k + 1]);
         }
       }
     }
@@ -282,7 +284,7 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp,
     }
 #pragma unroll
     for (int k = 0; k < 2 * kMaxSlots; ++k)
-      if (k < 2 * ns) no_uturn = no_uturn && (dot[k] >= 0.0);
+      if (k < 2 * ns) no_uturn = no_uturn && (dot[k] >= 0.f);
   }
   const double l2 = w.lw[lwi(w, c, j)];
   double energy = l2 - 0.5 * kin;                         // nuts.py:871-876
@@ -330,7 +332,7 @@ __global__ void nuts_depth_end_kernel(NutsDev w, uint2 key, int depth) {
   if (isnan(thresh)) thresh = 0.0;
   const float U = draw_uniform(key, draw_site(kDrawTreeUniform, depth, 0), (uint32_t)c);
   const bool choose = (log1p(-(double)U) <= thresh) && sub_cont;
-  double dl = 0.0, dr = 0.0;
+  float dl = 0.f, dr = 0.f;   // trajectory U-turn dots, FP32 as in the reference
   for (int d = lane; d < D; d += 32) {
     if (choose) {
       w.cand_q[o + d] = w.sub_q[o + d];
@@ -338,8 +340,8 @@ __global__ void nuts_depth_end_kernel(NutsDev w, uint2 key, int depth) {
     }
     const float ms = w.mom_sum[o + d] + w.cumsum[o + d];
     w.mom_sum[o + d] = ms;
-    dl += (double)ms * (double)w.end_p[0][o + d];
-    dr += (double)ms * (double)w.end_p[1][o + d];
+    dl = fmaf(ms, w.end_p[0][o + d], dl);
+    dr = fmaf(ms, w.end_p[1][o + d], dr);
   }
   dl = warp_sum(dl);
   dr = warp_sum(dr);
@@ -427,20 +429,20 @@ __global__ void hmc_finish_kernel(HmcDev w, const float* __restrict__ q0,
   if (c >= w.C) return;
   const float e = eps_of(eps, per_chain, c), he = 0.5f * e;
   const size_t o = (size_t)c * w.D;
-  double k0 = 0.0, k1 = 0.0;
+  float k0l = 0.f, k1l = 0.f;   // per-lane FP32 shares of |p|^2, summed in FP64
   for (int d = lane; d < w.D; d += 32) {
     const float g = w.gw[o + d];
     const float p1 = (w.ph[o + d] + e * g) - he * g;
     const float p0 = w.p0[o + d];
-    k0 += (double)p0 * (double)p0;
-    k1 += (double)p1 * (double)p1;
+    k0l = fmaf(p0, p0, k0l);
+    k1l = fmaf(p1, p1, k1l);
     if (out.final_momentum) out.final_momentum[o + d] = p1;
     if (out.initial_momentum) out.initial_momentum[o + d] = p0;
     if (out.proposed_state) out.proposed_state[o + d] = w.qw[o + d];
     if (out.proposed_grads) out.proposed_grads[o + d] = g;
   }
-  k0 = warp_sum(k0);
-  k1 = warp_sum(k1);
+  const double k0 = warp_sum((double)k0l);
+  const double k1 = warp_sum((double)k1l);
   const double l1 = w.lw[c];
   double corr = k0 - k1;                                  // hmc.py:861-875
   corr = isfinite(corr) ? 0.5 * corr : -INFINITY;

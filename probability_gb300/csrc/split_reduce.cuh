@@ -55,7 +55,29 @@ split_reduce_kernel(const double* __restrict__ lpart, const float* __restrict__ 
 #pragma unroll
   for (int k = 0; k < kK; ++k) acc[k] = 0.f;
   double lp = 0.0;
-  for (int s = warp; s < S; s += kReduceWarps) {
+  // Four splits' loads in flight per warp step (same summation order).
+  int s = warp;
+  for (; s + 3 * kReduceWarps < S; s += 4 * kReduceWarps) {
+    float v[4][kK];
+    double l4[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const size_t base = (size_t)(s + u * kReduceWarps) * sstride;
+#pragma unroll
+      for (int k = 0; k < kK; ++k) {
+        const int d = lane + 32 * k;
+        v[u][k] = d < D ? p[base + d] : 0.f;
+      }
+      l4[u] = lane == 0 ? lpart[(size_t)(s + u * kReduceWarps) * n + c] : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+#pragma unroll
+      for (int k = 0; k < kK; ++k) acc[k] += v[u][k];
+      lp += l4[u];
+    }
+  }
+  for (; s < S; s += kReduceWarps) {
 #pragma unroll
     for (int k = 0; k < kK; ++k) {
       const int d = lane + 32 * k;
