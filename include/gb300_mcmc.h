@@ -143,6 +143,20 @@ GBM_API int gbm_target_batch_layout(const gbm_target* target, int64_t* offsets, 
  * > 1024 (0: no member in that class). */
 GBM_API int gbm_target_batch_schedule(const gbm_target* target, int32_t chain_tile[4]);
 
+/* The target `inner` seen through one elementwise bijector per state
+ * dimension, for TransformedTransitionKernel (mcmc/transformed_kernel.py:165;
+ * the transformed log-density of make_transformed_log_prob,
+ * transformed_kernel.py:63-95): states x are unconstrained, `inner` is
+ * evaluated at y = f(x), and log |f'(x)| (float64) is added with the chain
+ * rule applied to the gradient.  bijector[d] is GBM_BIJECTOR_* (the forward
+ * maps of bijectors/exp.py, softplus.py, sigmoid.py).  `inner` must outlive
+ * the returned target and must not be a batch target. */
+#define GBM_BIJECTOR_IDENTITY 0
+#define GBM_BIJECTOR_EXP 1
+#define GBM_BIJECTOR_SOFTPLUS 2
+#define GBM_BIJECTOR_SIGMOID 3
+GBM_API int gbm_target_transformed(gbm_target* inner, const int32_t* bijector, gbm_target** out);
+
 GBM_API int gbm_target_destroy(gbm_target* target);
 GBM_API int gbm_target_dim(const gbm_target* target, int64_t* dim);
 

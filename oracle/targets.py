@@ -102,3 +102,36 @@ class NonCentredHierarchicalNormal:
     g[:, 1] = -2.0 * t * t / (1.0 + t * t) + 1.0 + tau * np.sum(r * z, -1)
     g[:, 2:] = -z + tau[:, None] * r
     return logp, g
+
+
+class TransformedTarget:
+  """A target seen through one elementwise bijector per dimension, the
+  transformed log-density TransformedTransitionKernel samples
+  (mcmc/transformed_kernel.py:63-95 make_transformed_log_prob with the
+  forward maps of bijectors/exp.py, softplus.py, sigmoid.py):
+  log p(f(x)) + sum_d log |f_d'(x_d)|.  Codes: 0 identity, 1 exp,
+  2 softplus, 3 sigmoid."""
+
+  def __init__(self, inner, codes):
+    self.inner = inner
+    self.codes = np.asarray(codes, np.int64)
+    self.dim = self.codes.shape[0]
+
+  def forward(self, x):
+    x = np.asarray(x, np.float64)
+    c = self.codes
+    return np.where(c == 1, np.exp(x), np.where(c == 2, softplus(x),
+                                                np.where(c == 3, sigmoid(x), x)))
+
+  def __call__(self, x):
+    x = np.asarray(x, np.float64)
+    c = self.codes
+    lp, gy = self.inner(self.forward(x))
+    s = sigmoid(x)
+    # f'(x), log f'(x) and d/dx log f'(x) per bijector
+    fp = np.where(c == 1, np.exp(x), np.where(c == 2, s, np.where(c == 3, s * (1 - s), 1.0)))
+    logfp = np.where(c == 1, x, np.where(c == 2, -softplus(-x),
+                                         np.where(c == 3, -softplus(-x) - softplus(x), 0.0)))
+    dlogfp = np.where(c == 1, 1.0, np.where(c == 2, 1.0 - s, np.where(c == 3, 1.0 - 2.0 * s,
+                                                                      0.0)))
+    return lp + logfp.sum(-1), gy * fp + dlogfp

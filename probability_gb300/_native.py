@@ -42,6 +42,7 @@ _SIGNATURES = {
     'gbm_target_logistic_regression': (
         [P, P, ctypes.c_int, I64, I64, P, F32, ctypes.c_int, ctypes.POINTER(P)], ctypes.c_int),
     'gbm_target_destroy': ([P], ctypes.c_int),
+    'gbm_target_transformed': ([P, P, ctypes.POINTER(P)], ctypes.c_int),
     'gbm_target_mvn': ([P, P, P, I64, F64, ctypes.POINTER(P)], ctypes.c_int),
     'gbm_target_hierarchical_normal': ([P, P, P, I64, F32, F32, ctypes.POINTER(P)],
                                        ctypes.c_int),

@@ -260,6 +260,25 @@ int gbm_target_batch(gbm_context* ctx, const gbm_batch_member* m, int64_t count,
   });
 }
 
+int gbm_target_transformed(gbm_target* inner, const int32_t* bijector, gbm_target** out) {
+  if (!inner || !bijector || !out) return invalid("gbm_target_transformed: NULL argument");
+  if (inner->impl->ragged_chains())
+    return invalid("gbm_target_transformed: batch targets are not supported");
+  for (int64_t d = 0; d < inner->impl->dim; ++d)
+    if (bijector[d] < GBM_BIJECTOR_IDENTITY || bijector[d] > GBM_BIJECTOR_SIGMOID)
+      return invalid("gbm_target_transformed: bijector codes are GBM_BIJECTOR_*");
+  gbm_context* ctx = inner->ctx;
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    std::unique_ptr<gbm_target> t(new gbm_target());
+    t->ctx = ctx;
+    t->impl = gbm::make_transformed(ctx, inner->impl.get(), bijector);
+    finish_target(ctx, t.get(), out);
+    t.release();
+    return GBM_OK;
+  });
+}
+
 int gbm_target_batch_layout(const gbm_target* t, int64_t* offsets, int32_t* dims,
                             int64_t* chains, int64_t* elements) {
   if (!t) return invalid("gbm_target_batch_layout: NULL target");

@@ -121,6 +121,8 @@ std::unique_ptr<Target> make_batch(gbm_context* ctx, const ::gbm_batch_member* m
 // Chain tiles chosen by the batch autotuner (false: `t` is not a batch).
 bool batch_schedule(const Target* t, int32_t* chain_tile);
 
+std::unique_ptr<Target> make_transformed(gbm_context* ctx, Target* inner, const int32_t* codes);
+
 std::unique_ptr<Target> make_logreg_simt(gbm_context* ctx, const float* X, int64_t n,
                                          int64_t d, const float* y, float prior_scale);
 

@@ -9,6 +9,8 @@ from probability_gb300.mcmc.metropolis_hastings import MetropolisHastingsKernelR
 from probability_gb300.mcmc.nuts import NoUTurnSampler, NUTSKernelResults
 from probability_gb300.mcmc.sample import (ChainRun, CheckpointableStatesAndTrace,
                                            StatesAndTrace, run_chain, sample_chain)
+from probability_gb300.mcmc.transformed_kernel import (TransformedTransitionKernel,
+                                                       TransformedTransitionKernelResults)
 from probability_gb300.mcmc.simple_step_size_adaptation import (
     hmc_like_log_accept_prob_getter_fn, hmc_like_step_size_getter_fn,
     hmc_like_step_size_setter_fn)
@@ -17,6 +19,7 @@ __all__ = [
     'ChainRun', 'run_chain', 'CheckpointableStatesAndTrace', 'DualAveragingStepSizeAdaptation',
     'DualAveragingStepSizeAdaptationResults', 'HamiltonianMonteCarlo',
     'MetropolisHastingsKernelResults', 'NUTSKernelResults', 'NoUTurnSampler', 'StatesAndTrace',
+    'TransformedTransitionKernel', 'TransformedTransitionKernelResults',
     'TransitionKernel', 'UncalibratedHamiltonianMonteCarlo',
     'UncalibratedHamiltonianMonteCarloKernelResults', 'effective_sample_size',
     'hmc_like_log_accept_prob_getter_fn', 'hmc_like_step_size_getter_fn',

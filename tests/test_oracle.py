@@ -227,3 +227,21 @@ def test_ess_iid_and_ar1():
 
 def test_sample_chain_step_count():
   assert mcmc.num_transitions(10, 5, 2) == 5 + 1 + 9 * 3
+
+
+def test_transformed_target_gradient_finite_difference():
+  """TransformedTarget (transformed_kernel.py:63-95): log p(f(x)) + log|f'(x)|
+  and its gradient, for every bijector, against central differences."""
+  rng = np.random.default_rng(11)
+  X = rng.normal(size=(40, 6))
+  X[:, 0] = 1
+  y = (rng.uniform(size=40) < 0.5).astype(float)
+  t = targets.TransformedTarget(targets.LogisticRegression(X, y), [0, 1, 2, 3, 1, 0])
+  x = rng.normal(size=(3, 6)) * 0.7
+  lp, g = t(x)
+  eps = 1e-6
+  for d in range(6):
+    e = np.zeros(6)
+    e[d] = eps
+    np.testing.assert_allclose(g[:, d], (t(x + e)[0] - t(x - e)[0]) / (2 * eps), rtol=1e-6,
+                               atol=1e-6)
