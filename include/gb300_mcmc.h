@@ -253,6 +253,20 @@ GBM_API int gbm_nuts_set_profiling(gbm_nuts* kernel, int enable);
  * same bits as per-leaf launches.  No reference counterpart: tfp.mcmc runs
  * under tf.function/XLA, which this replaces. */
 GBM_API int gbm_nuts_set_graphs(gbm_nuts* kernel, int enable);
+/* Diagonal mass matrix for subsequent gbm_nuts_one_step calls, as
+ * tfp.experimental.mcmc.PreconditionedNoUTurnSampler
+ * (experimental/mcmc/preconditioned_nuts.py:169) with the momentum
+ * distribution DiagonalMassMatrixAdaptation builds
+ * (experimental/mcmc/preconditioning_utils.py:40-97): precision diag(v),
+ * i.e. momentum p ~ N(0, diag(1/v)), velocity v * p, kinetic energy
+ * 1/2 sum v p^2, U-turn checks against velocities.  `inverse_mass` is v, a
+ * device pointer read by every later step (keep it alive; it may be
+ * updated in place): float32 [dim] shared by all chains, or with per_chain
+ * one value per state element.  NULL restores the identity (the
+ * NoUTurnSampler of nuts.py).  The energy reported excludes the momentum
+ * distribution's normalizer. */
+GBM_API int gbm_nuts_set_inverse_mass(gbm_nuts* kernel, const float* inverse_mass,
+                                      int per_chain);
 GBM_API int gbm_nuts_read_profile(gbm_nuts* kernel, double* eval_ms, int64_t* evals,
                                   int64_t* kernel_launches);
 

@@ -53,16 +53,19 @@ def safe_sum(xs, alt_value=-np.inf):
 # --------------------------------------------------------------------------
 
 
-def leapfrog(target, p, q, logp, grad, eps, num_steps, dtype=np.float64):
+def leapfrog(target, p, q, logp, grad, eps, num_steps, dtype=np.float64, inv_mass=None):
   """SimpleLeapfrogIntegrator.__call__: half kick, num_steps x (drift, grad,
   kick), final -half kick correction (leapfrog_integrator.py:280-316,
   319-362).  ``eps`` broadcasts against ``[C, D]`` (per-chain step = [C, 1]).
+  With ``inv_mass`` (diagonal M^-1), the drift moves by the velocity
+  M^-1 p (leapfrog_integrator.py:267-275, 330-335).
   """
   eps = np.asarray(eps, dtype)
   half = np.asarray(0.5, dtype) * eps
+  im = 1.0 if inv_mass is None else np.asarray(inv_mass, dtype)
   p_half = (p + half * grad).astype(dtype)
   for _ in range(num_steps):
-    q = (q + eps * p_half).astype(dtype)
+    q = (q + eps * (p_half * im)).astype(dtype)
     logp, grad = target(q)
     logp = logp.astype(dtype)
     grad = grad.astype(dtype)
@@ -171,11 +174,18 @@ def _has_not_u_turn(diff, p_left, p_right):
 
 def nuts_one_step(target, state, logp, grad, step_size, draws, max_tree_depth=10,
                   max_energy_diff=1000.0, unrolled_leapfrog_steps=1,
-                  dtype=np.float64):
+                  dtype=np.float64, inv_mass=None):
   """NoUTurnSampler.one_step (nuts.py:321-445) with _loop_tree_doubling
   (:541-711), _build_sub_tree/_loop_build_sub_tree (:713-946) and
   has_not_u_turn_at_all_index (:949-984).  Multinomial sampling, generalised
-  U-turn (the reference's static configuration, nuts.py:53-67)."""
+  U-turn (the reference's static configuration, nuts.py:53-67).
+
+  ``inv_mass`` (diagonal M^-1, [D] or [C, D]) gives PreconditionedNoUTurnSampler
+  (experimental/mcmc/preconditioned_nuts.py:169) with the momentum
+  distribution of preconditioning_utils.py:40-97 (precision = inv_mass):
+  p = z / sqrt(inv_mass), kinetic energy 1/2 sum inv_mass p^2, drift by the
+  velocity inv_mass p, U-turn dot products against velocities (:964-1030).
+  The energy excludes the momentum distribution's normalizer."""
   C, D = state.shape
   write, read = write_read_instruction(max_tree_depth)
   n_slots = int(write.max()) + 1
@@ -185,8 +195,11 @@ def nuts_one_step(target, state, logp, grad, step_size, draws, max_tree_depth=10
   s = np.asarray(step_size, dtype)
   eps_abs = np.full((C, 1), s, dtype) if s.ndim == 0 else s.reshape(C, 1)
 
+  im = np.ones(D, dtype) if inv_mass is None else np.asarray(inv_mass, dtype)
   p0 = draws.momentum((C, D)).astype(dtype)                        # :512-529
-  e0 = logp - 0.5 * np.sum(p0 * p0, -1)                             # :1085-1102
+  if inv_mass is not None:
+    p0 = (p0 / np.sqrt(im)).astype(dtype)
+  e0 = logp - 0.5 * np.sum(im * p0 * p0, -1)                        # :1085-1102
   # trajectory ends [left, right] (:352-361)
   ends = dict(p=np.stack([p0, p0]), q=np.stack([state, state]),
               l=np.stack([logp, logp]), g=np.stack([grad, grad]))
@@ -224,19 +237,21 @@ def nuts_one_step(target, state, logp, grad, step_size, draws, max_tree_depth=10
       if not sub_cont.any():
         break
       p1, q1, l1, g1 = leapfrog(target, cur['p'], cur['q'], cur['l'], cur['g'],
-                                eps, unrolled_leapfrog_steps, dtype)
+                                eps, unrolled_leapfrog_steps, dtype,
+                                None if inv_mass is None else im)
       cumsum_prev = cumsum
       cumsum = cumsum + p1                                          # :827-828
       sub_lf = np.where(sub_cont, sub_lf + 1, sub_lf)               # :829-830
       no_uturn = np.ones(C, bool)                                   # :846-855
+      v1 = p1 * im                                                  # velocity
       for i in range(int(read[leaf, 0]), int(read[leaf, 1])):
         diff = cumsum - slot_cs[i]
-        no_uturn &= _has_not_u_turn(diff, slot_p[i], p1)
+        no_uturn &= _has_not_u_turn(diff, slot_p[i], v1)
       w = int(write[leaf])                                          # :857-869
-      slot_p[w] = p1
+      slot_p[w] = v1
       slot_cs[w] = cumsum_prev
       energy = l1.astype(np.float64) - 0.5 * np.sum(
-          p1.astype(np.float64) ** 2, -1)                           # :871-876
+          im * p1.astype(np.float64) ** 2, -1)                      # :871-876
       energy = np.where(np.isnan(energy), -np.inf, energy)
       with np.errstate(invalid='ignore'):
         energy_diff = energy - e0
@@ -278,7 +293,7 @@ def nuts_one_step(target, state, logp, grad, step_size, draws, max_tree_depth=10
     for k in ends:
       ends[k][side, ar] = cur[k]
     momentum_sum = momentum_sum + cumsum
-    no_uturn_traj = _has_not_u_turn(momentum_sum, ends['p'][0], ends['p'][1])
+    no_uturn_traj = _has_not_u_turn(momentum_sum, ends['p'][0] * im, ends['p'][1] * im)
     is_accepted = choose | is_accepted
     continue_tree = sub_cont & no_uturn_traj
     not_divergence = sub_nd

@@ -568,6 +568,22 @@ int gbm_nuts_set_graphs(gbm_nuts* k, int enable) {
   return GBM_OK;
 }
 
+int gbm_nuts_set_inverse_mass(gbm_nuts* k, const float* inverse_mass, int per_chain) {
+  if (!k) return invalid("gbm_nuts_set_inverse_mass: NULL kernel");
+  if (k->dev.ragged && inverse_mass && !per_chain)
+    return invalid("gbm_nuts_set_inverse_mass: batch targets need a per-chain (ragged) array");
+  return guarded([&] {
+    if (k->inv_mass != inverse_mass || k->im_per_chain != (per_chain != 0)) {
+      // Captured graphs hold the pointer: capture again.
+      GBM_CUDA(cudaStreamSynchronize(k->ctx->stream));
+      gbm::nuts_clear_graphs(k);
+    }
+    k->inv_mass = inverse_mass;
+    k->im_per_chain = per_chain != 0;
+    return GBM_OK;
+  });
+}
+
 int gbm_nuts_read_profile(gbm_nuts* k, double* eval_ms, int64_t* evals, int64_t* launches) {
   if (!k || !eval_ms || !evals || !launches) return invalid("gbm_nuts_read_profile: NULL argument");
   return guarded([&] {

@@ -56,6 +56,10 @@ __device__ __forceinline__ size_t boff(const NutsDev& w, int c, int j) {
   return w.ragged ? (size_t)w.coff[c] : (size_t)j * w.D;
 }
 __device__ __forceinline__ int lwi(const NutsDev& w, int c, int j) { return w.ragged ? c : j; }
+// Inverse mass of element d of the chain whose vector starts at o (1: identity).
+__device__ __forceinline__ float imass(const NutsDev& w, size_t o, int d) {
+  return w.inv_mass ? (w.im_per_chain ? w.inv_mass[o + d] : w.inv_mass[d]) : 1.f;
+}
 
 // --------------------------------------------------------------------------
 // Active-chain compaction: idx[0..count) = chains with (flags & bit), sorted.
@@ -127,14 +131,17 @@ __global__ void nuts_init_kernel(NutsDev w, const float* __restrict__ q,
   const uint32_t site = draw_site(kDrawMomentum, 0, 0);
   float kin_l = 0.f;   // this lane's share of |p|^2 (FP32); summed across lanes in FP64
   for (int d = lane; d < D; d += 32) {
-    const float p = draw_normal(key, site, (uint32_t)(o + d));
+    const float im = imass(w, o, d);
+    // p ~ N(0, M): z / sqrt(M^-1) (preconditioned_nuts.py momentum draw)
+    const float p = w.inv_mass ? draw_normal(key, site, (uint32_t)(o + d)) / sqrtf(im)
+                               : draw_normal(key, site, (uint32_t)(o + d));
     const float qd = q[o + d], gd = g[o + d];
     w.end_q[0][o + d] = qd; w.end_q[1][o + d] = qd;
     w.end_p[0][o + d] = p;  w.end_p[1][o + d] = p;
     w.end_g[0][o + d] = gd; w.end_g[1][o + d] = gd;
     w.cand_q[o + d] = qd;   w.cand_g[o + d] = gd;
     w.mom_sum[o + d] = p;
-    kin_l = fmaf(p, p, kin_l);
+    kin_l = fmaf(p * im, p, kin_l);     // p^T M^-1 p
   }
   const double kin = warp_sum((double)kin_l);
   if (lane == 0) {
@@ -191,7 +198,7 @@ __global__ void nuts_leaf_pre_kernel(NutsDev w) {
   const float* G = w.end_g[side];
   for (int d = lane; d < D; d += 32) {
     const float ph = P[o + d] + he * G[o + d];
-    const float qn = Q[o + d] + e * ph;
+    const float qn = Q[o + d] + e * (ph * imass(w, o, d));   // drift by the velocity
     P[o + d] = ph;
     Q[o + d] = qn;
     w.qw[oj + d] = qn;
@@ -209,7 +216,7 @@ __global__ void nuts_leaf_mid_kernel(NutsDev w) {
   const int D = vdim(w, c);
   for (int d = lane; d < D; d += 32) {
     const float ph = w.end_p[side][o + d] + e * w.gw[oj + d];
-    const float qn = w.end_q[side][o + d] + e * ph;
+    const float qn = w.end_q[side][o + d] + e * (ph * imass(w, o, d));
     w.end_p[side][o + d] = ph;
     w.end_q[side][o + d] = qn;
     w.qw[oj + d] = qn;
@@ -243,12 +250,13 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp,
     const float csp = w.cumsum[o + d];
     const float cs = csp + p2;                          // nuts.py:827-828
     w.cumsum[o + d] = cs;
+    const float im = imass(w, o, d);
     if (wslot >= 0) {                                   // nuts.py:857-869
       const size_t so = soff(w, c, wslot) + d;
-      w.slot_p[so] = p2;
+      w.slot_p[so] = p2 * im;                           // velocity (preconditioned_nuts.py:877-885)
       w.slot_cs[so] = csp;
     }
-    kin_l = fmaf(p2, p2, kin_l);
+    kin_l = fmaf(p2 * im, p2, kin_l);
   }
   const double kin = warp_sum((double)kin_l);
   __syncwarp();
@@ -265,7 +273,7 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp,
 #pragma unroll
     for (int k = 0; k < 2 * kMaxSlots; ++k) dot[k] = 0.f;
     for (int d = lane; d < D; d += 32) {
-      const float cs = w.cumsum[o + d], pd = P[o + d];
+      const float cs = w.cumsum[o + d], pd = P[o + d] * imass(w, o, d);   // velocity
 #pragma unroll
       for (int k = 0; k < kMaxSlots; ++k) {
         if (k < ns) {
@@ -340,8 +348,9 @@ __global__ void nuts_depth_end_kernel(NutsDev w, uint2 key, int depth) {
     }
     const float ms = w.mom_sum[o + d] + w.cumsum[o + d];
     w.mom_sum[o + d] = ms;
-    dl = fmaf(ms, w.end_p[0][o + d], dl);
-    dr = fmaf(ms, w.end_p[1][o + d], dr);
+    const float im = imass(w, o, d);
+    dl = fmaf(ms, w.end_p[0][o + d] * im, dl);         // momentum sum . velocities
+    dr = fmaf(ms, w.end_p[1][o + d] * im, dr);
   }
   dl = warp_sum(dl);
   dr = warp_sum(dr);
@@ -627,6 +636,11 @@ void nuts_setup(gbm_nuts* k) {
   k->use_graphs = true;
 }
 
+void nuts_clear_graphs(gbm_nuts* k) {
+  for (auto& g : k->graphs) cudaGraphExecDestroy(g.second);
+  k->graphs.clear();
+}
+
 void nuts_release_graphs(gbm_nuts* k) {
   for (auto& g : k->graphs) cudaGraphExecDestroy(g.second);
   k->graphs.clear();
@@ -676,6 +690,8 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
   cudaStream_t s = ctx->stream;
   NutsDev w = k->dev;
   w.C = (int)chains;
+  w.inv_mass = k->inv_mass;
+  w.im_per_chain = k->im_per_chain;
   int* host_flags = ctx->host_flags;
   const int wb = warp_blocks(chains), tb = 256;
   const uint2* keyp = k->key_dev.as<uint2>();

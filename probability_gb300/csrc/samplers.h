@@ -30,6 +30,11 @@ struct NutsDev {
   int ragged;
   const int64_t* coff;      // [C] element offsets (ragged)
   const int* cdim;          // [C] dimensions (ragged)
+  // Diagonal inverse mass matrix (PreconditionedNoUTurnSampler): NULL for
+  // the identity, else [D] shared by every chain or, with im_per_chain, one
+  // entry per state element (the layout of the states).
+  const float* inv_mass;
+  int im_per_chain;
   float* end_q[2];
   float* end_p[2];
   float* end_g[2];
@@ -142,6 +147,8 @@ struct gbm_nuts {
   // use; the transition key is read from key_dev so graphs are reused by
   // every transition.
   bool use_graphs = false;
+  const float* inv_mass = nullptr;   // see NutsDev
+  int im_per_chain = 0;
   cudaStream_t graph_stream = nullptr;   // capture stream (graphs launch on the caller's)
   std::map<int64_t, cudaGraphExec_t> graphs;   // (chains, depth, first leaf)
   gbm::DeviceBuffer key_dev;   // uint2
@@ -160,6 +167,7 @@ struct gbm_nuts {
 namespace gbm {
 void nuts_profile_flush(gbm_nuts* k);  // stream must be synchronized
 void nuts_release_graphs(gbm_nuts* k);
+void nuts_clear_graphs(gbm_nuts* k);   // keep the capture stream
 }  // namespace gbm
 
 struct gbm_hmc {

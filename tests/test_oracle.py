@@ -245,3 +245,15 @@ def test_transformed_target_gradient_finite_difference():
     e[d] = eps
     np.testing.assert_allclose(g[:, d], (t(x + e)[0] - t(x - e)[0]) / (2 * eps), rtol=1e-6,
                                atol=1e-6)
+
+
+def test_running_variance_merges_batches():
+  """experimental/stats RunningVariance: batched (Chan) updates equal the
+  variance of all samples."""
+  torch = pytest.importorskip('torch')
+  from probability_gb300.experimental.stats import RunningVariance
+  x = torch.from_numpy(np.random.default_rng(0).normal(size=(97, 4)) * [1, 2, 3, 4])
+  rv = RunningVariance.from_shape((4,))
+  for a, b in [(0, 10), (10, 11), (11, 60), (60, 97)]:
+    rv = rv.update(x[a:b], axis=0)
+  np.testing.assert_allclose(rv.variance().numpy(), x.var(0, unbiased=False).numpy(), rtol=1e-12)
