@@ -619,7 +619,7 @@ def run_batch(args, w):
   import torch
   import probability_gb300 as pg
   from probability_gb300 import _native
-  from probability_gb300.batch import MemberDualAveraging
+  from probability_gb300.batch import MemberDualAveraging, MemberMassMatrixAdaptation
   world, rank, local = dist_setup(args)
   if rank != 0:
     return
@@ -642,11 +642,20 @@ def run_batch(args, w):
   k = pg.BatchedNoUTurnSampler(batch, da.step_size, max_tree_depth=w['depth'])
   kr = k.bootstrap_results(q)
   t = 0
-  for _ in range(args.warm_in):            # per-posterior dual averaging
+  # Warm-in: per-posterior dual averaging throughout; with preconditioning,
+  # each posterior's diagonal metric is estimated over the middle third and
+  # used from then on (a windowed adaptation, as windowed_sampling.py's).
+  mm = MemberMassMatrixAdaptation(batch) if args.precondition else None
+  w0, w1 = args.warm_in // 3, 2 * args.warm_in // 3
+  for i in range(args.warm_in):
     q, kr = k.one_step(q, kr._replace(step_size=batch.per_chain(da.step_size)),
                        seed=pg._util.step_key((w['seed'], 0), t))
     da.update(kr.log_accept_ratio)
     t += 1
+    if mm is not None and w0 <= i < w1:
+      mm.update(q)
+    if mm is not None and i == w1 - 1:
+      k.set_inverse_mass(mm.inverse_mass())
   eps = batch.per_chain(da.step_size)
   kr = kr._replace(step_size=eps)
   for _ in range(args.warmup):
@@ -712,6 +721,7 @@ def run_batch(args, w):
                  'max_tree_depth': w['depth'], 'warm_in_transitions': args.warm_in,
                  'step_size': 'one per posterior, dual averaging (target %.2f) in the warm-in'
                               % w['target_accept'],
+                 'preconditioned': bool(args.precondition),
                  'chain_tile_schedule': batch.schedule(),
                  'l2': 'flushed between timed steps (256 MB write outside the step events)'},
       'sum_min_ess_per_s': (ess_sum / secs) if ess_sum is not None else None,
@@ -832,6 +842,8 @@ def main():
                   help='transitions of the plain FP32 form timed beside the mixed path')
   ap.add_argument('--kernel-only', action='store_true',
                   help='time the batched log-prob+gradient alone (profiling aid)')
+  ap.add_argument('--precondition', action='store_true',
+                  help='nuts_batch_256: learn a diagonal metric per posterior in the warm-in')
   ap.add_argument('--kernel-rows', type=int, default=0,
                   help='with --kernel-only: rows of X (default: the workload\'s)')
   args = ap.parse_args()

@@ -167,6 +167,23 @@ class BatchedNoUTurnSampler:
     _native.check(_native.lib().gbm_nuts_set_graphs(h, int(bool(use_graphs))),
                   'gbm_nuts_set_graphs')
     self.last_leaf_iterations = 0
+    self.inverse_mass = None
+
+  def set_inverse_mass(self, inverse_mass):
+    """Diagonal inverse mass matrix (the preconditioning of
+    PreconditionedNoUTurnSampler) for the following steps: a ragged float32
+    vector with one entry per state element, or None for the identity."""
+    if inverse_mass is None:
+      self.inverse_mass = None
+      ptr = None
+    else:
+      v = _util.as_tensor(inverse_mass, torch.float32).reshape(-1).contiguous()
+      if v.numel() != self.batch.elements:
+        raise ValueError('inverse_mass needs one entry per state element')
+      self.inverse_mass = v              # kept alive while the engine reads it
+      ptr = _native.ptr(v)
+    _native.check(_native.lib().gbm_nuts_set_inverse_mass(self._handle, ptr, 1),
+                  'gbm_nuts_set_inverse_mass')
 
   def __del__(self):
     if getattr(self, '_handle', None) is not None and _native._lib is not None:
@@ -221,6 +238,46 @@ class BatchedNoUTurnSampler:
         target_log_prob=nl, grads_target_log_prob=ng, step_size=eps, log_accept_ratio=lar,
         leapfrogs_taken=lf, is_accepted=acc.bool(), reach_max_depth=rmd.bool(),
         has_divergence=div.bool(), energy=energy, seed=_util.seed_tensor(seed))
+
+
+class MemberMassMatrixAdaptation:
+  """DiagonalMassMatrixAdaptation (experimental/mcmc/
+  diagonal_mass_matrix_adaptation.py:73) for every member of a batch: the
+  running variance of each member's state, per dimension, with every chain
+  and step a sample, expanded to the ragged per-element inverse mass.  Two
+  scatter-adds per update whatever the number of members."""
+
+  def __init__(self, batch):
+    dev = _util.device()
+    self.batch = batch
+    g, base = [], 0
+    for c, d in zip(batch.member_chains, batch.member_dims):
+      g.append(np.tile(np.arange(base, base + d), c))
+      base += d
+    self.groups = base
+    self.index = torch.from_numpy(np.concatenate(g)).to(dev)
+    self.reset()
+
+  def reset(self):
+    dev = self.index.device
+    self.s1 = torch.zeros(self.groups, dtype=torch.float64, device=dev)
+    self.s2 = torch.zeros(self.groups, dtype=torch.float64, device=dev)
+    self.count = torch.zeros(self.groups, dtype=torch.float64, device=dev)
+    self._ones = torch.ones(self.index.shape[0], dtype=torch.float64, device=dev)
+
+  def update(self, state):
+    x = state.reshape(-1).to(torch.float64)
+    self.s1.index_add_(0, self.index, x)
+    self.s2.index_add_(0, self.index, x * x)
+    self.count.index_add_(0, self.index, self._ones)
+
+  def variance(self):
+    mean = self.s1 / self.count
+    return (self.s2 / self.count - mean * mean).clamp_min(1e-12)
+
+  def inverse_mass(self):
+    """The variance as a ragged float32 inverse mass (one entry per element)."""
+    return self.variance()[self.index].to(torch.float32)
 
 
 class MemberDualAveraging:
