@@ -638,6 +638,24 @@ def run_batch(args, w):
   q = batch.pack([torch.from_numpy((rng.normal(size=(c, t.event_dim)) * 0.5)
                                    .astype(np.float32)) for t, c in members]).to(dev)
   setup_s = time.perf_counter() - t_setup
+  if args.kernel_only:   # the full-population gradient alone (profiling aid)
+    for _ in range(args.warmup):
+      batch.log_prob_and_grad(q)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(batch.stream)
+    for _ in range(args.steps):
+      batch.log_prob_and_grad(q)
+    e1.record(batch.stream)
+    e1.synchronize()
+    ms = e0.elapsed_time(e1) / args.steps
+    flops = sum(2.0 * t.event_dim ** 2 * c if isinstance(t, pg.MultivariateNormalTriL)
+                else 10.0 * t.groups * c for t, c in members)
+    print(json.dumps({'kernel_only': True, 'workload': args.workload, 'ms_per_eval': ms,
+                      'tflops': flops / ms / 1e9, 'chains': batch.chains,
+                      'schedule': batch.schedule()}), flush=True)
+    return
   da = MemberDualAveraging(batch, 0.1, args.warm_in, target_accept_prob=w['target_accept'])
   k = pg.BatchedNoUTurnSampler(batch, da.step_size, max_tree_depth=w['depth'])
   kr = k.bootstrap_results(q)
@@ -850,7 +868,7 @@ def main():
   w = WORKLOADS[args.workload]
   if args.impl == 'reference':
     run_reference(args, w)
-  elif args.kernel_only:
+  elif args.kernel_only and not args.workload.startswith('nuts_batch'):
     run_kernel_only(args, w)
   elif args.workload.startswith('hmc_'):
     run_hmc(args, w)
