@@ -253,6 +253,13 @@ GBM_API int gbm_nuts_set_profiling(gbm_nuts* kernel, int enable);
  * same bits as per-leaf launches.  No reference counterpart: tfp.mcmc runs
  * under tf.function/XLA, which this replaces. */
 GBM_API int gbm_nuts_set_graphs(gbm_nuts* kernel, int enable);
+/* Streaming moments on the device (for the running potential scale
+ * reduction of experimental/mcmc/potential_scale_reduction_reducer.py and
+ * diagnostic.py:476-568 without storing draws): fold one state of
+ * `elements` float32 values into per-element running means and sums of
+ * squared deviations (float64, Welford) after `count_before` samples. */
+GBM_API int gbm_moments_update(gbm_context* ctx, const float* state, int64_t elements,
+                               int64_t count_before, double* mean, double* m2);
 /* Diagonal mass matrix for subsequent gbm_nuts_one_step calls, as
  * tfp.experimental.mcmc.PreconditionedNoUTurnSampler
  * (experimental/mcmc/preconditioned_nuts.py:169) with the momentum
@@ -371,6 +378,11 @@ typedef struct gbm_job_spec {
   int32_t* trace_leapfrogs_taken; /* [num_results][chains] */
   float* final_state;             /* [chains][dim] */
   float* final_step_size;         /* [1] */
+  /* optional streaming moments of the draws (float64 [chains][dim] each):
+   * per-chain mean and sum of squared deviations, for R-hat without the
+   * trace (gbm_moments_update) */
+  double* moments_mean;
+  double* moments_m2;
 } gbm_job_spec;
 
 typedef struct gbm_job_info {

@@ -58,6 +58,7 @@ _SIGNATURES = {
     'gbm_nuts_last_leaf_iterations': ([P, ctypes.POINTER(I64)], ctypes.c_int),
     'gbm_nuts_set_profiling': ([P, ctypes.c_int], ctypes.c_int),
     'gbm_nuts_set_graphs': ([P, ctypes.c_int], ctypes.c_int),
+    'gbm_moments_update': ([P, P, I64, I64, P, P], ctypes.c_int),
     'gbm_nuts_set_inverse_mass': ([P, P, ctypes.c_int], ctypes.c_int),
     'gbm_nuts_read_profile': ([P, ctypes.POINTER(F64), ctypes.POINTER(I64),
                                ctypes.POINTER(I64)], ctypes.c_int),

@@ -519,7 +519,7 @@ int gbm_nuts_sample_chain(gbm_nuts* k, int64_t chains, float* state, double* tlp
                                    step_count_smoothing, decay_rate, num_adaptation_steps},
                      nullptr, da_state};
     gbm::ChainTrace tr{trace_state, trace_tlp, trace_lar, trace_lf, trace_acc, trace_div,
-                       trace_eps};
+                       trace_eps, nullptr, nullptr};
     gbm::nuts_sample_chain(k, chains, state, tlp, grads, step_size, per_chain,
                            make_uint2(seed[0], seed[1]), (uint32_t)first_step, num_results,
                            burnin, thin, da, tr);
@@ -548,7 +548,8 @@ int gbm_hmc_sample_chain(gbm_hmc* k, int64_t chains, float* state, double* tlp, 
                      gbm::DaParams{target_accept_prob, exploration_shrinkage,
                                    step_count_smoothing, decay_rate, num_adaptation_steps},
                      nullptr, da_state};
-    gbm::ChainTrace tr{trace_state, trace_tlp, trace_lar, nullptr, trace_acc, nullptr, trace_eps};
+    gbm::ChainTrace tr{trace_state, trace_tlp, trace_lar, nullptr, trace_acc, nullptr, trace_eps,
+                       nullptr, nullptr};
     gbm::hmc_sample_chain(k, chains, state, tlp, grads, step_size, per_chain, num_leapfrog_steps,
                           make_uint2(seed[0], seed[1]), (uint32_t)first_step, num_results, burnin,
                           thin, da, tr);
@@ -560,6 +561,17 @@ int gbm_nuts_set_profiling(gbm_nuts* k, int enable) {
   if (!k) return invalid("gbm_nuts_set_profiling: NULL argument");
   k->profiling = enable != 0;
   return GBM_OK;
+}
+
+int gbm_moments_update(gbm_context* ctx, const float* state, int64_t elements,
+                       int64_t count_before, double* mean, double* m2) {
+  if (!ctx || !state || !mean || !m2) return invalid("gbm_moments_update: NULL argument");
+  if (elements <= 0 || count_before < 0) return invalid("gbm_moments_update: bad sizes");
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    gbm::moments_update(ctx->stream, state, (size_t)elements, count_before, mean, m2);
+    return GBM_OK;
+  });
 }
 
 int gbm_nuts_set_graphs(gbm_nuts* k, int enable) {

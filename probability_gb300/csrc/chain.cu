@@ -53,6 +53,25 @@ LoopBuffers carve(DeviceBuffer& mem, int64_t C, int64_t D) {
 
 }  // namespace
 
+__global__ void moments_update_kernel(const float* __restrict__ x, size_t n, double inv_count,
+                                      double* __restrict__ mean, double* __restrict__ m2) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double v = (double)x[i];
+  const double delta = v - mean[i];
+  const double mnew = mean[i] + delta * inv_count;
+  mean[i] = mnew;
+  m2[i] += delta * (v - mnew);
+}
+
+void moments_update(cudaStream_t s, const float* x, size_t n, int64_t count_before, double* mean,
+                    double* m2) {
+  if (!mean || !m2 || n == 0) return;
+  moments_update_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(
+      x, n, 1.0 / (double)(count_before + 1), mean, m2);
+  GBM_CUDA(cudaGetLastError());
+}
+
 void nuts_sample_chain(gbm_nuts* k, int64_t C, float* q, double* l, float* g, float* eps,
                        int per_chain, uint2 seed, uint32_t first_step, int64_t num_results,
                        int64_t burnin, int64_t thin, const DaConfig& da, const ChainTrace& tr) {
@@ -82,6 +101,7 @@ void nuts_sample_chain(gbm_nuts* k, int64_t C, float* q, double* l, float* g, fl
     copy_row(tr.is_accepted ? tr.is_accepted + r * C : nullptr, b.acc, C, s);
     copy_row(tr.has_divergence ? tr.has_divergence + r * C : nullptr, b.div, C, s);
     copy_row(tr.step_size ? tr.step_size + r * groups : nullptr, eps, groups, s);
+    moments_update(s, cq, vec, r, tr.moment_mean, tr.moment_m2);
   }
   if (cq != q) {  // the final state lives in the scratch buffers: hand it back
     copy_row(q, cq, vec, s);

@@ -93,7 +93,17 @@ struct ChainTrace {
   uint8_t* is_accepted;       // [R][C]
   uint8_t* has_divergence;    // [R][C] (NUTS)
   float* step_size;           // [R][groups]
+  // Streaming moments of the traced states (Welford, float64 [C][D]): the
+  // per-chain running mean and sum of squared deviations over the results,
+  // for diagnostics without storing the draws.
+  double* moment_mean;
+  double* moment_m2;
 };
+
+// Fold one state [n elements] into running moments after `count_before`
+// earlier samples (Welford).
+void moments_update(cudaStream_t s, const float* x, size_t n, int64_t count_before, double* mean,
+                    double* m2);
 
 // Dual-averaging configuration of a chain loop (enabled = 0: fixed step).
 struct DaConfig {

@@ -152,7 +152,11 @@ void run_job(gbm_context* ctx, Job* job) {
                DaParams{s.target_accept_prob, 0.05, 10.0, 0.75, s.num_adaptation_steps}, nullptr,
                da.as<double>()};
   ChainTrace tr{s.trace_state, nullptr, s.trace_log_accept_ratio, s.trace_leapfrogs_taken,
-                nullptr, nullptr, nullptr};
+                nullptr, nullptr, nullptr, s.moments_mean, s.moments_m2};
+  if (s.moments_mean && s.moments_m2) {
+    GBM_CUDA(cudaMemsetAsync(s.moments_mean, 0, sizeof(double) * C * D, st));
+    GBM_CUDA(cudaMemsetAsync(s.moments_m2, 0, sizeof(double) * C * D, st));
+  }
   nuts_sample_chain(&k, C, q.as<float>(), l.as<double>(), g.as<float>(), eps.as<float>(), 0,
                     make_uint2(s.seed[0], s.seed[1]), 0, s.num_results, s.num_burnin_steps, 0, dac,
                     tr);

@@ -32,6 +32,7 @@ class JobSpec(ctypes.Structure):
       ('num_results', ctypes.c_int64), ('num_burnin_steps', ctypes.c_int64),
       ('seed', ctypes.c_uint32 * 2), ('trace_state', P), ('trace_log_accept_ratio', P),
       ('trace_leapfrogs_taken', P), ('final_state', P), ('final_step_size', P),
+      ('moments_mean', P), ('moments_m2', P),
   ]
 
 
@@ -144,6 +145,9 @@ class Server:
       outs['log_accept_ratio'] = torch.empty((R, C), dtype=torch.float64, device=dev)
     if 'leapfrogs_taken' in trace:
       outs['leapfrogs_taken'] = torch.empty((R, C), dtype=torch.int32, device=dev)
+    if 'moments' in trace:   # streaming per-chain mean / squared deviations of the draws
+      outs['moments_mean'] = torch.empty((C, D), dtype=torch.float64, device=dev)
+      outs['moments_m2'] = torch.empty((C, D), dtype=torch.float64, device=dev)
     seed = _util.sanitize_seed(seed)
     spec.dim, spec.chains, spec.init_state = D, C, _native.ptr(q)
     spec.step_size = float(step_size)
@@ -155,6 +159,8 @@ class Server:
     spec.trace_state = _native.ptr(outs.get('states'))
     spec.trace_log_accept_ratio = _native.ptr(outs.get('log_accept_ratio'))
     spec.trace_leapfrogs_taken = _native.ptr(outs.get('leapfrogs_taken'))
+    spec.moments_mean = _native.ptr(outs.get('moments_mean'))
+    spec.moments_m2 = _native.ptr(outs.get('moments_m2'))
     spec.final_state = _native.ptr(outs['final_state'])
     spec.final_step_size = _native.ptr(outs['final_step_size'])
     # Inputs were written on this thread's torch stream; the workers use their
