@@ -64,6 +64,15 @@ __global__ void moments_update_kernel(const float* __restrict__ x, size_t n, dou
   m2[i] += delta * (v - mnew);
 }
 
+// The key of the transition at the device-side step counter, then advance it
+// (so a captured transition can be replayed for every step).
+__global__ void advance_step_key_kernel(uint2 seed, uint32_t* step, uint2* key) {
+  *key = step_key(seed, *step);
+  *step += 1;
+}
+
+__global__ void set_step_kernel(uint32_t* step, uint32_t v) { *step = v; }
+
 void moments_update(cudaStream_t s, const float* x, size_t n, int64_t count_before, double* mean,
                     double* m2) {
   if (!mean || !m2 || n == 0) return;
@@ -121,15 +130,43 @@ void hmc_sample_chain(gbm_hmc* k, int64_t C, float* q, double* l, float* g, floa
   float *cq = q, *cg = g, *nq = b.q, *ng = b.g;
   double *cl = l, *nl = b.l;
   const int64_t groups = per_chain ? C : 1;
-  uint32_t t = first_step;
+  // A transition is a fixed launch sequence: key from the device step
+  // counter, the leapfrogs, the MH finish, dual averaging.  With graphs it is
+  // captured once for each of the two ping-pong buffer assignments and
+  // replayed for every step.
+  uint2* keyp = k->key_dev.as<uint2>();
+  uint32_t* stepp = reinterpret_cast<uint32_t*>(keyp + 1);
+  set_step_kernel<<<1, 1, 0, s>>>(stepp, first_step);
+  GBM_CUDA(cudaGetLastError());
+  auto transition = [&](float* iq, double* il, float* ig, float* oq, double* ol, float* og,
+                        cudaStream_t ls) {
+    advance_step_key_kernel<<<1, 1, 0, ls>>>(seed, stepp, keyp);
+    HmcOutputs out{oq, ol, og, nullptr, nullptr, nullptr, nullptr, nullptr,
+                   b.corr, b.lar, b.acc};
+    hmc_step_launches(k, C, iq, il, ig, eps, per_chain, num_leapfrog_steps, keyp, out, ls);
+    if (da.enabled)
+      dual_averaging_update(ls, b.lar, C, per_chain, da.prm, da.target_accept, da.state, eps);
+  };
+  cudaGraphExec_t graphs[2] = {nullptr, nullptr};
+  cudaStream_t cs = nullptr;
+  if (k->use_graphs) GBM_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
   for (int64_t r = 0; r < num_results; ++r) {
     const int64_t n = (r == 0) ? 1 + burnin : 1 + thin;
-    for (int64_t i = 0; i < n; ++i, ++t) {
-      HmcOutputs out{nq, nl, ng, nullptr, nullptr, nullptr, nullptr, nullptr,
-                     b.corr, b.lar, b.acc};
-      hmc_one_step(k, C, cq, cl, cg, eps, per_chain, num_leapfrog_steps, step_key(seed, t), out);
-      if (da.enabled)
-        dual_averaging_update(s, b.lar, C, per_chain, da.prm, da.target_accept, da.state, eps);
+    for (int64_t i = 0; i < n; ++i) {
+      if (cs) {
+        const int parity = cq == q ? 0 : 1;
+        if (!graphs[parity]) {
+          cudaGraph_t graph;
+          GBM_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+          transition(cq, cl, cg, nq, nl, ng, cs);
+          GBM_CUDA(cudaStreamEndCapture(cs, &graph));
+          GBM_CUDA(cudaGraphInstantiate(&graphs[parity], graph, 0));
+          GBM_CUDA(cudaGraphDestroy(graph));
+        }
+        GBM_CUDA(cudaGraphLaunch(graphs[parity], s));
+      } else {
+        transition(cq, cl, cg, nq, nl, ng, s);
+      }
       std::swap(cq, nq);
       std::swap(cl, nl);
       std::swap(cg, ng);
@@ -144,6 +181,12 @@ void hmc_sample_chain(gbm_hmc* k, int64_t C, float* q, double* l, float* g, floa
     copy_row(q, cq, vec, s);
     copy_row(g, cg, vec, s);
     copy_row(l, cl, C, s);
+  }
+  if (cs) {
+    GBM_CUDA(cudaStreamSynchronize(s));   // replays finished before the graphs go
+    for (auto& gx : graphs)
+      if (gx) cudaGraphExecDestroy(gx);
+    cudaStreamDestroy(cs);
   }
 }
 

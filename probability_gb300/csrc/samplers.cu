@@ -402,7 +402,9 @@ struct HmcDev {
 };
 
 __global__ void hmc_init_kernel(HmcDev w, const float* __restrict__ q, const float* __restrict__ g,
-                                const float* __restrict__ eps, int per_chain, uint2 key) {
+                                const float* __restrict__ eps, int per_chain,
+                                const uint2* __restrict__ keyp) {
+  const uint2 key = *keyp;
   const int c = warp_id(), lane = threadIdx.x & 31;
   if (c >= w.C) return;
   if (c == 0 && lane == 0) *w.count = w.C;
@@ -432,8 +434,10 @@ __global__ void hmc_kick_drift_kernel(HmcDev w, const float* __restrict__ eps, i
 
 __global__ void hmc_finish_kernel(HmcDev w, const float* __restrict__ q0,
                                   const double* __restrict__ l0, const float* __restrict__ g0,
-                                  const float* __restrict__ eps, int per_chain, uint2 key,
+                                  const float* __restrict__ eps, int per_chain,
+                                  const uint2* __restrict__ keyp,
                                   HmcOutputs out) {
+  const uint2 key = *keyp;
   const int c = warp_id(), lane = threadIdx.x & 31;
   if (c >= w.C) return;
   const float e = eps_of(eps, per_chain, c), he = 0.5f * e;
@@ -789,12 +793,21 @@ void hmc_setup(gbm_hmc* k) {
   const size_t vec = (size_t)C * D;
   k->mem.reserve(sizeof(float) * vec * 4 + sizeof(double) * C + 256 + sizeof(int) * 64);
   k->target_ws.reserve(k->target->impl->workspace_bytes(C));
+  k->key_dev.reserve(16);
 }
 
 void hmc_one_step(gbm_hmc* k, int64_t chains, const float* q, const double* l, const float* g,
                   const float* eps, int per_chain, int num_leapfrog_steps, uint2 key,
                   const HmcOutputs& out) {
   cudaStream_t s = k->target->ctx->stream;
+  uint2* keyp = k->key_dev.as<uint2>();
+  set_key_kernel<<<1, 1, 0, s>>>(keyp, key);
+  hmc_step_launches(k, chains, q, l, g, eps, per_chain, num_leapfrog_steps, keyp, out, s);
+}
+
+void hmc_step_launches(gbm_hmc* k, int64_t chains, const float* q, const double* l,
+                       const float* g, const float* eps, int per_chain, int num_leapfrog_steps,
+                       const uint2* keyp, const HmcOutputs& out, cudaStream_t s) {
   const int64_t D = k->target->impl->dim;
   const size_t vec = (size_t)k->max_chains * D;
   float* fv = k->mem.as<float>();
@@ -808,14 +821,14 @@ void hmc_one_step(gbm_hmc* k, int64_t chains, const float* q, const double* l, c
   w.lw = reinterpret_cast<double*>(fv + 4 * vec);
   w.count = reinterpret_cast<int*>(w.lw + k->max_chains);
   const int wb = warp_blocks(chains);
-  hmc_init_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, q, g, eps, per_chain, key);
+  hmc_init_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, q, g, eps, per_chain, keyp);
   GBM_CUDA(cudaGetLastError());
   for (int i = 0; i < num_leapfrog_steps; ++i) {
     k->target->impl->eval(w.qw, w.D, w.count, w.C, w.lw, w.gw, w.D, k->target_ws.ptr, s);
     if (i + 1 < num_leapfrog_steps)
       hmc_kick_drift_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, eps, per_chain);
   }
-  hmc_finish_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, q, l, g, eps, per_chain, key, out);
+  hmc_finish_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, q, l, g, eps, per_chain, keyp, out);
   GBM_CUDA(cudaGetLastError());
 }
 

@@ -123,6 +123,10 @@ void nuts_setup(gbm_nuts* k);
 void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l, const float* g,
                    const float* eps, int eps_per_chain, uint2 key, const NutsOutputs& out);
 void hmc_setup(gbm_hmc* k);
+// Launches of one HMC transition with the key read from device memory.
+void hmc_step_launches(gbm_hmc* k, int64_t chains, const float* q, const double* l,
+                       const float* g, const float* eps, int per_chain, int num_leapfrog_steps,
+                       const uint2* keyp, const HmcOutputs& out, cudaStream_t s);
 void hmc_one_step(gbm_hmc* k, int64_t chains, const float* q, const double* l, const float* g,
                   const float* eps, int per_chain, int num_leapfrog_steps, uint2 key,
                   const HmcOutputs& out);
@@ -187,4 +191,6 @@ struct gbm_hmc {
   gbm::DeviceBuffer mem;
   gbm::DeviceBuffer target_ws;
   gbm::DeviceBuffer loop_mem;   // chain-loop ping-pong and result buffers
+  gbm::DeviceBuffer key_dev;    // uint2 transition key + uint32 step counter
+  bool use_graphs = true;       // device loops replay each transition as a graph
 };
