@@ -622,6 +622,33 @@ def make_batch_members(w):
   return spec
 
 
+def cpu_batch_gradient_rate(spec, max_seconds, sample=16, seed=0):
+  """grad-evals/s of the oracle's log-density + gradient (NumPy, all host
+  threads) over a seeded sample of the posteriors, each with its own chains:
+  the NUTS leaf cost of those members on the CPU."""
+  from oracle import targets as ot
+  rng = np.random.default_rng(seed)
+  pick = rng.choice(len(spec), size=min(sample, len(spec)), replace=False)
+  members = []
+  for i in pick:
+    s = spec[i]
+    t = ot.MultivariateNormalTriL(s[1], s[2]) if s[0] == 'mvn' else \
+        ot.NonCentredHierarchicalNormal(s[1], s[2])
+    d = t.dim if s[0] == 'mvn' else len(s[1]) + 2
+    members.append((t, rng.normal(size=(s[3], d)) * 0.5))
+  evals, passes = 0, 0
+  t0 = time.perf_counter()
+  while True:
+    for t, x in members:
+      t(x)
+      evals += x.shape[0]
+    passes += 1
+    if time.perf_counter() - t0 > max_seconds:
+      break
+  dt = time.perf_counter() - t0
+  return evals / dt, passes, dt, [int(i) for i in pick]
+
+
 def run_batch(args, w):
   """256 uneven posteriors in one BatchedNoUTurnSampler."""
   import ctypes
@@ -736,6 +763,14 @@ def run_batch(args, w):
       ess_sum += float(ess.min().item())
   achieved = float(flops.item()) / secs / 1e12
   fp32_peak = 2 * 128 * 152 * 2.07e9 / 1e12     # FMA lanes x 2 flop x SMs x max clock
+  cpu = None
+  if not args.no_cpu_baseline:
+    budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '15'))
+    rate, passes, dt, pick = cpu_batch_gradient_rate(spec, budget)
+    cpu = {'value': rate, 'unit': 'grad-evals/s', 'cores': os.cpu_count(), 'kind': 'port',
+           'sample': '%d passes of the log-prob+gradient of 16 of the 256 posteriors with all '
+                     'their chains (%.1f s; the NUTS leaf cost, no tree bookkeeping); NumPy '
+                     'float64 oracle targets, BLAS threads = all cores' % (passes, dt)}
   line = {
       'metric': 'grad-evals/s over 256 uneven posteriors in one sampler (sum of min-ESS/s beside)',
       'value': grad_evals / secs, 'unit': 'grad-evals/s', 'n_gpus': 1, 'steps': args.steps,
@@ -758,6 +793,7 @@ def run_batch(args, w):
                    'kernel': 'batch_phase_kernel (whole sampler step timed)',
                    'peak_source': 'nominal FP32 FMA rate at the maximum SM clock'},
       'setup_s': setup_s, 'gpu_launches': int(la.value), 'clocks': clk,
+      'cpu_baseline': cpu,
   }
   print(json.dumps(line), flush=True)
 
