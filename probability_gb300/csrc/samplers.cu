@@ -25,7 +25,6 @@
 namespace gbm {
 
 constexpr int kWarpsPerBlock = 8;
-constexpr int kMaxSlots = 16;   // U-turn slots: max_tree_depth <= 16
 
 static inline int warp_blocks(int64_t n) {
   return (int)((n + kWarpsPerBlock - 1) / kWarpsPerBlock);
@@ -263,36 +262,21 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp,
   // Within-subtree U-turn over the read range (reads never hit wslot: a leaf
   // that ends subtrees writes only the dummy slot, which is skipped).  The
   // dot products are FP32, the state's type, as in the reference (GB300's
-  // FP64 pipe is narrow); every slot's two products are accumulated per lane
-  // first and then reduced across the warp together, so the shuffle
-  // latencies overlap.
+  // FP64 pipe is narrow); the slot loop stays rolled to keep registers (and
+  // occupancy over tens of thousands of chains) reasonable.
   bool no_uturn = true;
-  const int ns = r1 - r0;
-  if (ns > 0) {
-    float dot[2 * kMaxSlots];
-#pragma unroll
-    for (int k = 0; k < 2 * kMaxSlots; ++k) dot[k] = 0.f;
+#pragma unroll 1
+  for (int i = r0; i < r1; ++i) {
+    float dl = 0.f, dr = 0.f;
+    const size_t so = soff(w, c, i);
     for (int d = lane; d < D; d += 32) {
-      const float cs = w.cumsum[o + d], pd = P[o + d] * imass(w, o, d);   // velocity
-#pragma unroll
-      for (int k = 0; k < kMaxSlots; ++k) {
-        if (k < ns) {
-          const size_t so = soff(w, c, r0 + k) + d;
-          const float diff = cs - w.slot_cs[so];
-          dot[2 * k] = fmaf(diff, w.slot_p[so], dot[2 * k]);
-          dot[2 * k + 1] = fmaf(diff, pd, dot[2 * k + 1]);
-        }
-      }
+      const float diff = w.cumsum[o + d] - w.slot_cs[so + d];
+      dl = fmaf(diff, w.slot_p[so + d], dl);
+      dr = fmaf(diff, P[o + d] * imass(w, o, d), dr);   // velocity
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-#pragma unroll
-      for (int k = 0; k < 2 * kMaxSlots; ++k)
-        if (k < 2 * ns) dot[k] += __shfl_xor_sync(0xffffffffu, dot[k], off);
-    }
-#pragma unroll
-    for (int k = 0; k < 2 * kMaxSlots; ++k)
-      if (k < 2 * ns) no_uturn = no_uturn && (dot[k] >= 0.f);
+    dl = warp_sum(dl);
+    dr = warp_sum(dr);
+    no_uturn = no_uturn && (dl >= 0.f) && (dr >= 0.f);
   }
   const double l2 = w.lw[lwi(w, c, j)];
   double energy = l2 - 0.5 * kin;                         // nuts.py:871-876
