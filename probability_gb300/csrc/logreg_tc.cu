@@ -3,31 +3,34 @@
 //
 // Same mathematics as logreg_simt.cu (the inference_gym logistic-regression
 // target, spinoffs/inference_gym/inference_gym/targets/logistic_regression.py:
-// 92-103; distributions/bernoulli.py:126-140), computed per 128-row tile as
-//   Z  = X_tile B^T          (M = 128 rows, N = chain tile, K = features)
-//   R  = y - sigmoid(Z),  logp += sum_rows log Bernoulli(y | Z)
-//   G += X_tile^T R          (M = 128 features, N = chain tile, K = 128 rows)
-// with BF16 operands and FP32 accumulation in TMEM.  X is BF16; the FP32
-// chain states B are split into a BF16 high part and a BF16 residual and
-// both are multiplied (residual correction), so Z -- and therefore the
-// log-density that drives acceptance -- carries ~16 significant bits of the
-// states.  R enters the gradient contraction as BF16.  A gradient that is a
+// 92-103; distributions/bernoulli.py:126-140): per 128-row tile of X and
+// tile of chains,
+//   Z = X_tile B^T,  R = y - sigmoid(Z),  logp += sum_rows log Bernoulli(y | Z),
+//   G += X_tile^T R,
+// with BF16 operands and FP32 accumulation in TMEM.  X is BF16 (plus a BF16
+// residual X_lo for FP32 data up to 128 features); the FP32 chain states B
+// are split into a BF16 high part and a BF16 residual and both are
+// multiplied (residual correction), so Z -- and therefore the log-density
+// that drives acceptance -- carries ~16 significant bits of the states.  R
+// enters the gradient contraction as BF16.  A gradient that is a
 // deterministic function of the state keeps the leapfrog map reversible and
 // volume-preserving, so the sampler stays exact; only its acceptance rate
 // depends on the gradient's accuracy.
 //
-// One X tile in shared memory (TMA, 128-byte swizzle, [64-feature block]
-// [128 rows][128 B]) is read by both MMAs: as the K-major A operand of the
-// first and, unchanged, as the MN-major A operand (X^T) of the second, so X is
-// read from HBM/L2 once per chain tile.
-//
-// Warp roles (320 threads): warp 0 issues TMA loads, warp 1 allocates TMEM
-// and issues the MMAs, warps 2-9 run the epilogue (two warps per TMEM lane
-// quarter, each on half of the chain tile).  X stages, Z accumulators and R
-// tiles are double-buffered, so GEMM1 of tile i+1 and GEMM2 of tile i run on
-// the tensor core while the epilogue works on tile i+1.  Every wait is
-// bounded (%globaltimer); on timeout the kernel records an error code, drains
-// what it issued and frees its TMEM.
+// Three kernels, by feature count:
+//   D <= 128        logreg_tct_kernel: chain-major (states and R in TMEM as
+//                   the A operand; one thread per chain in the epilogue);
+//   128 < D <= 256  logreg_tc_kernel: row-major (X tile as the A operand of
+//                   both contractions, R through shared memory);
+//   256 < D <= 512  logreg_tc_pair_kernel: a 2-CTA cluster splits the
+//                   features of the row-major form.
+// In all three one X tile in shared memory (TMA, 128-byte swizzle,
+// [64-feature block][128 rows][128 B]) serves both contractions, read K-major
+// by the first and MN-major by the second, so X is read from HBM/L2 once per
+// chain tile.  Warp 0 issues TMA loads, warp 1 allocates TMEM and issues the
+// MMAs, the other warps run the epilogue.  Every wait is bounded
+// (%globaltimer); on timeout a kernel records an error code, drains what it
+// issued and frees its TMEM.
 #include <cuda.h>
 #include <cuda_bf16.h>
 #include <cuda_runtime.h>
@@ -66,10 +69,10 @@ __host__ __device__ inline int tc_splits(int n, int ct, int grid, int row_tiles)
   return s > row_tiles ? row_tiles : s;
 }
 
-// Shared memory.  With up to 128 features, X_hi has three stages so that the
+// Shared memory of the row-major kernel (instantiated for 128 < D <= 256:
+// KB = 4, 64-chain tiles).  KB = 2 would give X_hi three stages, so that the
 // TMA refill of a stage (which can start only once GEMM2 has read it) runs a
-// full tile ahead of the GEMM1 that needs it; R is then single-buffered (the
-// epilogue waits for GEMM2 to release it only just before its first store).
+// full tile ahead of the GEMM1 that needs it, and a single R buffer.
 template <int KB, int CT, bool XLO>
 struct TcLayout {
   static constexpr int kStages = KB == 2 ? 3 : 2;      // X_hi stages
@@ -126,6 +129,13 @@ __device__ __forceinline__ bool wait_or_abort(uint64_t* bar, uint32_t parity,
     if (*abort_flag) return false;
     if (tc::globaltimer_ns() - t0 > kWaitLimitNs) return false;
   }
+}
+
+// wait_or_abort by every lane of a warp, with one outcome for the whole warp
+// (the .sync.aligned TMEM accesses that follow need a converged warp).
+__device__ __forceinline__ bool warp_wait(uint64_t* bar, uint32_t parity,
+                                          volatile int* abort_flag) {
+  return __all_sync(0xffffffffu, wait_or_abort(bar, parity, abort_flag));
 }
 
 // XLO: X is FP32 data stored as X_hi + X_lo (both BF16); GEMM1 adds the
@@ -460,6 +470,380 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
   if (warp == 1) {
     tc::tc_fence_after();
     tc::tmem_dealloc(tmem, L::kTmemCols);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// D <= 128, chain-major: the chain states stay in TMEM as the A operand of
+// both contractions, so every MMA reads only X from shared memory (half the
+// shared-memory traffic of the row-major form above):
+//   Z^T  = B X_tile^T        (M = 128 chains, N = 128 rows, K = features)
+//   R^T  = (y - sigmoid(Z))^T, BF16, written back to TMEM by the epilogue
+//   G^T += R^T X_tile        (M = 128 chains, N = features, K = 128 rows)
+// B is stored in TMEM as BF16 hi/lo (residual correction, as above); X_tile
+// is the same swizzled shared-memory tile, read K-major by the first MMA and
+// MN-major by the second.
+//
+// Each epilogue thread owns one chain (its TMEM lane) and 32 rows of a tile,
+// which changes the arithmetic per element:
+//   * sum_r ln(1 + e^-|z_r|) = ln prod_r (1 + e^-|z_r|): one lg2 per 32 rows
+//     (each factor is in (1, 2], so a product of 16 stays below 2^16);
+//   * sigmoid(|z|) = 1 / (1 + e^-|z|) by the hardware reciprocal;
+//   * the FP32 arithmetic around them runs two rows per instruction (packed
+//     f32x2), since instruction issue, not the multi-function unit, is the
+//     scarce resource of this epilogue.
+//
+// TMEM columns: B_hi [0, 64), B_lo [64, 128), two Z^T buffers [128, 256) and
+// [256, 384), G^T [384, 512).  R^T overwrites, in place, the first 16 of the
+// 32 Z^T columns the same warp has just loaded; each 16-row K-step of the
+// second contraction reads 8 adjacent columns, so R's scattered placement
+// costs nothing.  A Z buffer is refilled only after the contraction that
+// read its R has completed.  X (+ X_lo) and y have three shared-memory
+// stages.  Every wait is bounded.
+// ---------------------------------------------------------------------------
+constexpr int kTctEpi = 16;                 // epilogue warps: 4 lane quarters x 4 row blocks
+constexpr uint32_t kTBhi = 0, kTBlo = 64, kTZ = 128, kTG = 384;
+constexpr int kTctStride = 129;             // floats per row of the chain staging tile
+
+template <bool XLO>
+struct TctLayout {
+  static constexpr int kStages = 3;
+  static constexpr int kXStage = (XLO ? 2 : 1) * 32768;   // X [2][128][128 B] (+ X_lo)
+  static constexpr int kX = 0;
+  static constexpr int kY = kStages * kXStage;            // y - 1/2, [stages][128] float
+  static constexpr int kRed = kY + kStages * 512;         // [4 row blocks][128 chains] double
+  static constexpr int kCtl = kRed + 4 * 128 * 8;
+  static constexpr int kBytes = kCtl + 256;
+  // Before the first and after the last TMA load the X stages hold a
+  // [128 chains][kTctStride] float tile (states in, gradient out).
+  static_assert(128 * kTctStride * 4 <= kY, "chain staging tile must fit the X stages");
+  static_assert(kBytes + 1024 <= 232448, "shared memory over the sm_103a limit");
+};
+
+struct TctBars {
+  uint64_t x_full[3], x_empty[3], z_full[2], r_full[2], zr_free[2], g_done, drain;
+};
+
+__device__ __forceinline__ float2 f2(float a, float b) { return make_float2(a, b); }
+
+// -copysign(w, h): the magnitude of w with the sign of -h.
+__device__ __forceinline__ float neg_copysign(float w, float h) {
+  return __int_as_float((__float_as_int(w) & 0x7fffffff) |
+                        (~__float_as_int(h) & (int)0x80000000));
+}
+
+// 32 rows of one chain, two at a time.  With arg = -2 log2(e) |h|,
+// t = 2^arg = e^-|z| and u = 1 + t:
+//   *sarg += arg (so sum |h| = -sarg / (2 log2 e)),
+//   *prod *= u,
+//   R = (y - 1/2) - tanh(h)/2 with tanh(|h|)/2 = 1/u - 1/2 (rcp.approx,
+//     within one ulp), packed as BF16 pairs (round to nearest).
+// MASK: rows at or past `nvalid` are padding (X = 0) and leave both sums
+// unchanged.
+template <bool MASK>
+__device__ __forceinline__ void tct_rows(const float (&h)[32], const float* __restrict__ ys,
+                                         int nvalid, float2* sarg, float2* prod,
+                                         uint32_t (&rp)[16]) {
+  const float2 one = f2(1.f, 1.f), mhalf = f2(-0.5f, -0.5f);
+  float2 sa = f2(0.f, 0.f), pr = f2(1.f, 1.f);
+#pragma unroll
+  for (int g = 0; g < 8; ++g) {
+    const float4 yv = *reinterpret_cast<const float4*>(ys + 4 * g);
+#pragma unroll
+    for (int e = 0; e < 2; ++e) {
+      const int j = 4 * g + 2 * e;
+      float2 arg = f2(fabsf(h[j]) * kNeg2Log2e, fabsf(h[j + 1]) * kNeg2Log2e);
+      float2 u = __fadd2_rn(f2(tc::ex2_approx(arg.x), tc::ex2_approx(arg.y)), one);
+      if (MASK) {
+        if (j >= nvalid) { arg.x = 0.f; u.x = 1.f; }
+        if (j + 1 >= nvalid) { arg.y = 0.f; u.y = 1.f; }
+      }
+      sa = __fadd2_rn(sa, arg);
+      pr = __fmul2_rn(pr, u);
+      const float2 w = __fadd2_rn(f2(tc::rcp_approx(u.x), tc::rcp_approx(u.y)), mhalf);
+      const float2 ym = e == 0 ? f2(yv.x, yv.y) : f2(yv.z, yv.w);
+      const float2 r = __fadd2_rn(ym, f2(neg_copysign(w.x, h[j]), neg_copysign(w.y, h[j + 1])));
+      rp[2 * g + e] = pack_bf16x2(r.x, r.y);
+    }
+  }
+  *sarg = sa;
+  *prod = pr;
+}
+
+template <bool XLO>
+__global__ void __launch_bounds__(tc_threads(kTctEpi), 1)
+logreg_tct_kernel(const __grid_constant__ CUtensorMap xmap,
+                  const __grid_constant__ CUtensorMap xlomap, const float* __restrict__ ym,
+                  int N, int D, const float* __restrict__ Q, int ldq,
+                  const int* __restrict__ n_dev, int grid, double* __restrict__ lpart,
+                  float* __restrict__ gpart, int* __restrict__ err) {
+  using L = TctLayout<XLO>;
+  constexpr int CT = 128;
+  constexpr int kThreads = tc_threads(kTctEpi);
+  extern __shared__ __align__(1024) unsigned char smem_raw[];
+  unsigned char* smem = reinterpret_cast<unsigned char*>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  const int n = *n_dev;
+  const int row_tiles = (N + kRows - 1) / kRows;
+  const int S = tc_splits(n, CT, grid, row_tiles);
+  const int tiles = (n + CT - 1) / CT;
+  if (S == 0 || (int)blockIdx.x >= tiles * S) return;
+  const int tile = blockIdx.x % tiles, split = blockIdx.x / tiles;
+  const int c0 = tile * CT;
+  const int rt_begin = (int)((long long)split * row_tiles / S);
+  const int rt_end = (int)((long long)(split + 1) * row_tiles / S);
+  const int T = rt_end - rt_begin;
+  const int ksteps = (D + 15) >> 4;            // 16-feature K-steps holding data
+  const int nkb = (D + 63) >> 6;               // 64-feature blocks of X loaded
+
+  unsigned char* Xs = smem + L::kX;
+  float* stage_f = reinterpret_cast<float*>(smem + L::kX);   // [128][kTctStride] staging
+  float* Ys = reinterpret_cast<float*>(smem + L::kY);
+  double* red = reinterpret_cast<double*>(smem + L::kRed);
+  TctBars* bars = reinterpret_cast<TctBars*>(smem + L::kCtl);
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(smem + L::kCtl + sizeof(TctBars));
+  volatile int* abort_flag = reinterpret_cast<volatile int*>(tmem_slot + 1);
+
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  if (tid == 0) {
+    for (int i = 0; i < 3; ++i) {
+      tc::mbar_init(&bars->x_full[i], 1);
+      tc::mbar_init(&bars->x_empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      tc::mbar_init(&bars->z_full[i], 1);
+      tc::mbar_init(&bars->r_full[i], kTctEpi);
+      tc::mbar_init(&bars->zr_free[i], 1);
+    }
+    tc::mbar_init(&bars->g_done, 1);
+    tc::mbar_init(&bars->drain, 1);
+    *abort_flag = 0;
+    tc::fence_mbar_init();
+    tc::prefetch_tmap(&xmap);
+    if constexpr (XLO) tc::prefetch_tmap(&xlomap);
+  }
+  if (warp == 1) tc::tmem_alloc(tmem_slot, 512);
+  // Chain states / 2 (coalesced) -> staging tile; the factor 1/2 (exact)
+  // makes Z^T hold h = z / 2.
+  for (int i = tid; i < CT * 128; i += kThreads) {
+    const int cc = i >> 7, d = i & 127;
+    stage_f[cc * kTctStride + d] =
+        (c0 + cc < n && d < D) ? 0.5f * Q[(size_t)(c0 + cc) * ldq + d] : 0.f;
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+  const uint32_t tmem = *tmem_slot;
+
+  const int quarter = warp & 3;                // TMEM lanes 32*quarter .. (chains)
+  const int rblk = (warp - 2) >> 2;            // epilogue: rows / features [32 rblk, +32)
+  const uint32_t lane_base = (uint32_t)(quarter * 32) << 16;
+  const int c = quarter * 32 + lane;           // chain of this epilogue thread
+  if (warp >= 2) {
+    // BF16 hi/lo of this chain's 32 features -> TMEM (lane = chain, two
+    // features per column).
+    const float* src = stage_f + c * kTctStride + rblk * 32;
+    uint32_t hi[16], lo[16];
+#pragma unroll
+    for (int e = 0; e < 16; ++e) {
+      const float v0 = src[2 * e], v1 = src[2 * e + 1];
+      const __nv_bfloat162 hv = __floats2bfloat162_rn(v0, v1);
+      hi[e] = *reinterpret_cast<const uint32_t*>(&hv);
+      const float2 hf = __bfloat1622float2(hv);
+      lo[e] = pack_bf16x2(v0 - hf.x, v1 - hf.y);
+    }
+    tc::tmem_st16(tmem + lane_base + kTBhi + rblk * 16, hi);
+    tc::tmem_st16(tmem + lane_base + kTBlo + rblk * 16, lo);
+    tc::tmem_st_wait();
+  }
+  // The staging tile is overwritten by TMA next: order these generic-proxy
+  // accesses before the async-proxy writes.
+  tc::fence_proxy_async_smem();
+  tc::tc_fence_before();
+  __syncthreads();
+  tc::tc_fence_after();
+
+  if (warp == 0) {
+    // ---------------- TMA producer ----------------
+    if (lane == 0) {
+      const uint32_t bytes = (uint32_t)nkb * 16384u * (XLO ? 2u : 1u) + 512u;
+      int it = 0;
+      for (; it < T; ++it) {
+        const int s = it % L::kStages;
+        if (!wait_or_abort(&bars->x_empty[s], ((uint32_t)(it / L::kStages) & 1) ^ 1,
+                           abort_flag)) {
+          tc::record_error(err, kTcTimeoutTma);
+          *abort_flag = 1;
+          break;
+        }
+        const int r0 = (rt_begin + it) * kRows;
+        tc::mbar_arrive_expect_tx(&bars->x_full[s], bytes);
+        unsigned char* xs = Xs + s * L::kXStage;
+        for (int kb = 0; kb < nkb; ++kb) {
+          tc::tma_load_2d(xs + kb * 16384, &xmap, kb * 64, r0, &bars->x_full[s]);
+          if constexpr (XLO)
+            tc::tma_load_2d(xs + 32768 + kb * 16384, &xlomap, kb * 64, r0, &bars->x_full[s]);
+        }
+        tc::bulk_load(Ys + s * kRows, ym + r0, 512u, &bars->x_full[s]);
+      }
+      for (int j = (it > L::kStages ? it - L::kStages : 0); j < it; ++j)
+        tc::mbar_wait(&bars->x_full[j % L::kStages], (uint32_t)((j / L::kStages) & 1),
+                      kWaitLimitNs);
+    }
+  } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
+    if (lane == 0) {
+      const int nd = ksteps * 16;                                      // N of G^T
+      constexpr uint32_t idesc1 = tc::idesc_bf16_f32(128, 128, false, false);
+      const uint32_t idesc2 = tc::idesc_bf16_f32(128, nd, false, true);  // MN-major X
+      // Shared-memory descriptors are linear in the start address (bits 0-13
+      // hold address >> 4; every operand lies below 256 KB, so adding an
+      // offset >> 4 never carries out of the field): one base descriptor per
+      // major-ness, plus compile-time offsets in the unrolled loops.
+      const uint64_t xk = tc::smem_desc_sw128(tc::smem_u32(Xs), 16, 1024);     // K-major
+      const uint64_t xmn = tc::smem_desc_sw128(tc::smem_u32(Xs), 16384, 1024); // MN-major
+      bool ok = true;
+      auto gemm1 = [&](int it) -> bool {
+        const int s = it % L::kStages, b = it & 1;
+        if (!wait_or_abort(&bars->x_full[s], (uint32_t)(it / L::kStages) & 1, abort_flag))
+          return false;
+        tc::tc_fence_after();
+        const uint64_t xs = xk + (uint64_t)((s * L::kXStage) >> 4);
+        const uint32_t tz = tmem + kTZ + b * 128;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) {
+          if (k < ksteps) {
+            const uint64_t bx = xs + (uint64_t)(((k >> 2) * 16384 + (k & 3) * 32) >> 4);
+            tc::mma_bf16_tmem_a(tz, tmem + kTBhi + k * 8, bx, idesc1, k > 0 ? 1u : 0u);
+            tc::mma_bf16_tmem_a(tz, tmem + kTBlo + k * 8, bx, idesc1, 1u);
+            if constexpr (XLO)
+              tc::mma_bf16_tmem_a(tz, tmem + kTBhi + k * 8, bx + (32768 >> 4), idesc1, 1u);
+          }
+        }
+        tc::mma_commit(&bars->z_full[b]);
+        return true;
+      };
+      if (T > 0) ok = gemm1(0);
+      if (ok && T > 1) ok = gemm1(1);
+      for (int it = 0; it < T && ok; ++it) {
+        const int s = it % L::kStages, b = it & 1;
+        const uint32_t phase = (uint32_t)(it >> 1) & 1;
+        if (!wait_or_abort(&bars->r_full[b], phase, abort_flag)) {
+          ok = false;
+          break;
+        }
+        tc::tc_fence_after();
+        const uint64_t xs = xmn + (uint64_t)((s * L::kXStage) >> 4);
+        const uint32_t tr = tmem + kTZ + b * 128;
+#pragma unroll
+        for (int ks = 0; ks < kRows / 16; ++ks) {
+          // Rows 16 ks .. 16 ks + 15: row block ks / 2, half ks % 2.
+          tc::mma_bf16_tmem_a(tmem + kTG, tr + (ks >> 1) * 32 + (ks & 1) * 8,
+                              xs + (uint64_t)((ks * 2048) >> 4), idesc2,
+                              (it > 0 || ks > 0) ? 1u : 0u);
+        }
+        tc::mma_commit(&bars->x_empty[s]);
+        if (it + 2 < T) {
+          // Buffer b is refilled only after this contraction has read R.
+          tc::mma_commit(&bars->zr_free[b]);
+          if (!wait_or_abort(&bars->zr_free[b], phase, abort_flag)) {
+            ok = false;
+            break;
+          }
+          tc::tc_fence_after();
+          ok = gemm1(it + 2);
+        }
+      }
+      if (ok) {
+        tc::mma_commit(&bars->g_done);
+      } else {
+        tc::record_error(err, kTcTimeoutMma);
+        *abort_flag = 1;
+      }
+      tc::mma_commit(&bars->drain);
+      tc::mbar_wait(&bars->drain, 0, kWaitLimitNs);
+    }
+  } else {
+    // ---------------- epilogue (16 warps) ----------------
+    // Kahan sum over tiles of sum_r (|h_r| + ln(1 + e^-|z_r|)) for this
+    // chain's rows; the linear part sum_r (y_r - 1/2) z_r is added exactly by
+    // the reduction.
+    constexpr float kArgToAbsH = -1.f / 2.8853900817779268f;   // arg -> |h|
+    float acc = 0.f, comp = 0.f;
+    bool ok = true;
+    for (int it = 0; it < T; ++it) {
+      const int s = it % L::kStages, b = it & 1;
+      if (!warp_wait(&bars->z_full[b], (uint32_t)(it >> 1) & 1, abort_flag)) {
+        ok = false;
+        break;
+      }
+      tc::tc_fence_after();
+      const uint32_t tz = tmem + lane_base + kTZ + b * 128 + rblk * 32;
+      float h[32];
+      tc::tmem_ld32(tz, h);
+      tc::tmem_ld_wait();
+      // y of this tile: landed with X (already complete; the wait makes the
+      // bulk copy's writes visible to this thread).
+      if (!warp_wait(&bars->x_full[s], (uint32_t)(it / L::kStages) & 1, abort_flag)) {
+        ok = false;
+        break;
+      }
+      const int nvalid = N - ((rt_begin + it) * kRows + rblk * 32);
+      const float* ys = Ys + s * kRows + rblk * 32;
+      uint32_t rp[16];
+      float2 sarg, prod;
+      if (nvalid >= 32) tct_rows<false>(h, ys, 32, &sarg, &prod, rp);
+      else tct_rows<true>(h, ys, nvalid, &sarg, &prod, rp);
+      {
+        const float sabs = (sarg.x + sarg.y) * kArgToAbsH;
+        const float v = fmaf(kLn2, tc::lg2_approx(prod.x * prod.y), sabs) - comp;
+        const float t = acc + v;
+        comp = (t - acc) - v;
+        acc = t;
+      }
+      // R^T over the first 16 of this warp's 32 Z^T columns (already loaded).
+      tc::tmem_st16(tz, rp);
+      tc::tmem_st_wait();
+      tc::tc_fence_before();
+      __syncwarp();
+      if (lane == 0) tc::mbar_arrive(&bars->r_full[b]);
+    }
+    if (ok && T > 0) ok = warp_wait(&bars->g_done, 0, abort_flag);
+    if (!ok) {
+      tc::record_error(err, kTcTimeoutEpilogue);
+      *abort_flag = 1;
+    } else {
+      tc::tc_fence_after();
+      // G^T (lane = chain, column = feature) -> staging tile (the X stages
+      // are idle: every load has been consumed by the finished MMAs).
+      float g[32];
+      tc::tmem_ld32(tmem + lane_base + kTG + rblk * 32, g);
+      tc::tmem_ld_wait();
+      float* dst = stage_f + c * kTctStride + rblk * 32;
+#pragma unroll
+      for (int j = 0; j < 32; ++j) dst[j] = g[j];
+      red[rblk * CT + c] = -((double)acc - (double)comp);
+    }
+    named_barrier(1, 32 * kTctEpi);
+    if (ok) {
+      for (int cc = tid - 64; cc < CT; cc += 32 * kTctEpi) {
+        const double sum = red[cc] + red[CT + cc] + red[2 * CT + cc] + red[3 * CT + cc];
+        if (c0 + cc < n) lpart[(size_t)split * n + c0 + cc] = sum;
+      }
+      // Coalesced gradient partials: one warp per chain row at a time.
+      const int ew = warp - 2;
+      for (int cc = ew; cc < CT; cc += kTctEpi) {
+        if (c0 + cc >= n) break;
+        float* row = gpart + ((size_t)split * n + c0 + cc) * D;
+        for (int d = lane; d < D; d += 32) row[d] = stage_f[cc * kTctStride + d];
+      }
+    }
+  }
+  tc::tc_fence_before();
+  __syncthreads();
+  if (warp == 1) {
+    tc::tc_fence_after();
+    tc::tmem_dealloc(tmem, 512);
   }
 }
 
@@ -875,6 +1259,12 @@ __global__ void to_bf16_padded(const float* __restrict__ X, int64_t N, int D, in
   if (lo) lo[i] = __float2bfloat16_rn(v - __bfloat162float(h));
 }
 
+__global__ void y_minus_half(const float* __restrict__ y, int64_t N, int64_t padded,
+                             float* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < padded) out[i] = i < N ? y[i] - 0.5f : 0.f;
+}
+
 __global__ void bf16_pad(const __nv_bfloat16* __restrict__ X, int64_t N, int D, int Dp,
                          __nv_bfloat16* __restrict__ out) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -961,6 +1351,13 @@ class LogregTc final : public Target {
     GBM_CUDA(cudaGetLastError());
     GBM_CUDA(cudaMemcpyAsync(y_.ptr, y, sizeof(float) * N_, cudaMemcpyDeviceToDevice,
                              ctx->stream));
+    if (kb_ == 2) {
+      const int64_t padded = (N_ + kRows - 1) / kRows * kRows;
+      ym_.reserve(sizeof(float) * (size_t)padded);
+      y_minus_half<<<(unsigned)((padded + 255) / 256), 256, 0, ctx->stream>>>(y, N_, padded,
+                                                                              ym_.as<float>());
+      GBM_CUDA(cudaGetLastError());
+    }
     {
       const int nb = 2 * ctx->num_sms;
       const int64_t chunk = (N_ + nb - 1) / nb;
@@ -1000,12 +1397,12 @@ class LogregTc final : public Target {
     encode(&xlomap_, xlo_ ? xl_.ptr : xb_.ptr, Dp);
     const int attr = cudaFuncAttributeMaxDynamicSharedMemorySize;
     if (kb_ == 2 && xlo_) {
-      smem_ = TcLayout<2, 128, true>::kBytes + 1024;
-      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<2, 128, 16, true>, (cudaFuncAttribute)attr,
+      smem_ = TctLayout<true>::kBytes + 1024;
+      GBM_CUDA(cudaFuncSetAttribute(logreg_tct_kernel<true>, (cudaFuncAttribute)attr,
                                     (int)smem_));
     } else if (kb_ == 2) {
-      smem_ = TcLayout<2, 128, false>::kBytes + 1024;
-      GBM_CUDA(cudaFuncSetAttribute(logreg_tc_kernel<2, 128, 16, false>, (cudaFuncAttribute)attr,
+      smem_ = TctLayout<false>::kBytes + 1024;
+      GBM_CUDA(cudaFuncSetAttribute(logreg_tct_kernel<false>, (cudaFuncAttribute)attr,
                                     (int)smem_));
     } else if (kb_ == 4) {
       smem_ = TcLayout<4, 64, false>::kBytes + 1024;
@@ -1028,13 +1425,17 @@ class LogregTc final : public Target {
 #define GBM_TC_LAUNCH(KB_, CT_, EPI_, XLO_)                                               \
   logreg_tc_kernel<KB_, CT_, EPI_, XLO_><<<grid_, tc_threads(EPI_), smem_, s>>>(          \
       xmap_, xlomap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_dev_)
-    if (kb_ == 2 && xlo_) GBM_TC_LAUNCH(2, 128, 16, true);
-    else if (kb_ == 2) GBM_TC_LAUNCH(2, 128, 16, false);
+#define GBM_TCT_LAUNCH(XLO_)                                                              \
+  logreg_tct_kernel<XLO_><<<grid_, tc_threads(kTctEpi), smem_, s>>>(                       \
+      xmap_, xlomap_, ym_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_dev_)
+    if (kb_ == 2 && xlo_) GBM_TCT_LAUNCH(true);
+    else if (kb_ == 2) GBM_TCT_LAUNCH(false);
     else if (kb_ == 4) GBM_TC_LAUNCH(4, 64, 8, false);
     else
       logreg_tc_pair_kernel<<<2 * grid_, tc_threads(kPairEpi), smem_, s>>>(
           xmap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_dev_);
 #undef GBM_TC_LAUNCH
+#undef GBM_TCT_LAUNCH
     GBM_CUDA(cudaGetLastError());
     launch_split_reduce(lpart, gpart, q, ldq, n_dev, cap, ct_, kRows, grid_, N, D, inv_var_,
                         log_norm_, lin_.as<double>(), logp, grad, ldg, s);
@@ -1067,6 +1468,7 @@ class LogregTc final : public Target {
   }
 
   DeviceBuffer xb_, xl_, y_;
+  DeviceBuffer ym_;    // y - 1/2, zero-padded to whole row tiles (chain-major kernel)
   DeviceBuffer lin_;   // X^T (y - 1/2), float64 [D]
   bool xlo_ = false;
   CUtensorMap xlomap_;
