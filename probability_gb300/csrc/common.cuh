@@ -60,11 +60,30 @@ __device__ __forceinline__ double softplus_d(double x) {
 }
 
 // math/generic.py:585-612 log_add_exp: larger + softplus((x-l) + (y-l)).
-// Keeps the reference's NaN for (-inf, -inf).
+// Keeps the reference's NaN for (-inf, -inf).  The sum is float64; the
+// softplus term (argument <= 0, value in [0, ln 2]) is evaluated in float32,
+// an absolute error of ~1e-7: a float64 exp/log1p pair is ~60 instructions
+// on this GPU's narrow FP64 pipe, executed per chain per leaf.
 __device__ __forceinline__ double log_add_exp(double x, double y) {
   double l = fmax(x, y);
   if (isnan(x) || isnan(y)) l = x + y;  // propagate NaN like tf.maximum
-  return l + softplus_d((x - l) + (y - l));
+  const float d = (float)((x - l) + (y - l));
+  return l + (double)log1pf(expf(d));
+}
+
+// log(1 - U) for a float32 uniform U in [0, 1), in float32 (see log_add_exp).
+__device__ __forceinline__ double log1m_uniform(float U) { return (double)log1pf(-U); }
+
+// e^x for x <= 0 over the whole float64 range (down to the subnormals) with
+// float32 relative accuracy: e^x = 2^n 2^f with n = floor(x log2 e) applied
+// exactly by ldexp and 2^f, f in [0, 1), from exp2f.  Used where a float32
+// exponential would underflow (an acceptance probability e^-529 must still
+// give log_accept_ratio -529) but a float64 exp costs too much.
+__device__ __forceinline__ double exp_nonpositive(double x) {
+  if (!(x > -746.0)) return x != x ? x : 0.0;   // NaN stays NaN; below the range: 0
+  const double t = x * 1.4426950408889634;       // log2(e)
+  const double n = floor(t);
+  return ldexp((double)exp2f((float)(t - n)), (int)n);
 }
 
 }  // namespace gbm

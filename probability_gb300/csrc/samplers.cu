@@ -286,7 +286,7 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp,
   const double wsum = log_add_exp(w.sub_w[c], de);        // nuts.py:881-883
   const double thresh = de - wsum;
   const float U = draw_uniform(key, draw_site(kDrawLeafUniform, depth, leaf), (uint32_t)c);
-  const bool acc = log1p(-(double)U) <= thresh;           // nuts.py:897-901
+  const bool acc = log1m_uniform(U) <= thresh;           // nuts.py:897-901
   if (acc) {
     for (int d = lane; d < D; d += 32) {
       w.sub_q[o + d] = w.end_q[side][o + d];
@@ -298,7 +298,7 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp,
     if (acc) { w.sub_l[c] = l2; w.sub_e[c] = energy; }
     w.sub_w[c] = wsum;
     const bool cont = not_div;                            // previous was active
-    if (cont) w.sub_eds[c] += exp(fmin(de, 0.0));         // nuts.py:929-933
+    if (cont) w.sub_eds[c] += exp_nonpositive(fmin(de, 0.0));   // nuts.py:929-933
     w.sub_lf[c] += 1;                                     // nuts.py:829-830
     uint8_t nf = f;
     if (!not_div) nf &= (uint8_t)~kSubNotDiv;
@@ -323,7 +323,7 @@ __global__ void nuts_depth_end_kernel(NutsDev w, uint2 key, int depth) {
   double thresh = tree_w - cw;
   if (isnan(thresh)) thresh = 0.0;
   const float U = draw_uniform(key, draw_site(kDrawTreeUniform, depth, 0), (uint32_t)c);
-  const bool choose = (log1p(-(double)U) <= thresh) && sub_cont;
+  const bool choose = (log1m_uniform(U) <= thresh) && sub_cont;
   float dl = 0.f, dr = 0.f;   // trajectory U-turn dots, FP32 as in the reference
   for (int d = lane; d < D; d += 32) {
     if (choose) {
