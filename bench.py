@@ -461,7 +461,8 @@ def run_engine(args, w):
   achieved_tflops = alg_flops / eval_s / 1e12 if eval_s > 0 else None
   tensor_peak = peaks['bf16_tflops']
   kernel_name = ('logreg_partial_kernel' if target.precision == 'fp32' else
-                 'logreg_tc_pair_kernel' if w['d'] > 256 else 'logreg_tc_kernel')
+                 'logreg_tc_pair_kernel' if w['d'] > 256 else
+                 'logreg_tc_kernel' if w['d'] > 128 else 'logreg_tct_kernel')
   roofline = {
       'bound': 'tensor', 'achieved': achieved_tflops, 'peak': tensor_peak, 'unit': 'TFLOP/s',
       'frac': achieved_tflops / tensor_peak if achieved_tflops else None,
