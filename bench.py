@@ -435,9 +435,11 @@ def run_engine(args, w):
   # stream bracket every batched gradient evaluation (leaf-by-leaf launches)
   _native.check(_native.lib().gbm_nuts_set_profiling(nuts._handle, 1))
   lf_prof = torch.zeros((), dtype=torch.int64, device=dev)
+  leaves_prof = 0          # leaf iterations (batched evaluations) of the profiled pass
   for _ in range(args.steps):
     state, kr = step(state, kr, t)
     t += 1
+    leaves_prof += int(getattr(nuts, 'last_leaf_iterations', 0) or 0)
     lf_prof += kr.inner_results.leapfrogs_taken.sum()
   prof_ms, prof_evals, prof_la = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
   _native.check(_native.lib().gbm_nuts_read_profile(
@@ -452,6 +454,14 @@ def run_engine(args, w):
     ess = pg.mcmc.effective_sample_size(draws_t, filter_beyond_positive_pairs=True,
                                         cross_chain_dims=1)
     min_ess_per_s = float(ess.min().item()) / secs
+  # Split R-hat (diagnostic.py:339,517-543) over the timed draws, max over
+  # dimensions; a diagnostic of the short timed window, not a convergence claim.
+  rhat_max = None
+  if args.steps >= 4:
+    try:
+      rhat_max = float(pg.mcmc.potential_scale_reduction(draws_t, split_chains=True).max().item())
+    except Exception:   # a diagnostic must never fail the benchmark line
+      rhat_max = None
 
   # ---- roofline of the dominant kernel (batched gradient) ----
   flops_per_grad, bytes_per_batch = target.cost(1)
@@ -584,6 +594,15 @@ def run_engine(args, w):
                    'l2': 'flushed between timed steps (256 MB write outside the step events)',
                    'parallelism': 'replicas' if world > 1 else 'single'},
         'min_ess_per_s': min_ess_per_s,
+        'split_rhat_max_timed_draws': rhat_max,
+        # Lane-gradients over the profiled pass: the engine evaluates only the
+        # chains still building (compacted batches), so executed = useful; a
+        # lock-step implementation that masks finished chains evaluates
+        # chains x leaf iterations.
+        'lane_grads_profiled_pass': {
+            'useful': int(lf_prof.item()), 'executed': int(lf_prof.item()),
+            'lockstep_masked': w['chains'] * leaves_prof if leaves_prof else None,
+            'leaf_iterations': leaves_prof, 'transitions': args.steps},
         'step_size': float(kr.new_step_size.reshape(-1)[0].item()),
         'mean_leapfrogs_per_chain_step': grad_evals / (args.steps * w['chains'] * world),
         'wall_s_timed_region': wall,
