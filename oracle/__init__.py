@@ -3,7 +3,8 @@
 TEST INFRASTRUCTURE ONLY.  Nothing in the product package imports this
 directory; only ``tests/``, ``__graft_entry__.smoke()`` and the
 ``cpu_baseline`` / ``--impl reference`` legs of ``bench.py`` may use it, and
-only as the checker (or as the timed CPU restatement of the reference).
+only to check the engine's results (or as the timed CPU restatement of the
+reference).
 
 It is a NumPy restatement of TensorFlow Probability's ``tfp.mcmc`` algorithms
 (HamiltonianMonteCarlo, MetropolisHastings, SimpleLeapfrogIntegrator,
