@@ -65,6 +65,7 @@ WORKLOADS['serve_logreg_stream'] = dict(rate=200.0, requests=64, length_scale=0.
                                         depth=10, budget_gb=150, workers=16)
 METRIC = 'grad-evals/s (NUTS leapfrogs_taken summed over chains; min-ESS/s reported beside)'
 METRIC_HMC = 'grad-evals/s (HMC: chains x num_leapfrog_steps per transition; min-ESS/s beside)'
+METRIC_BATCH = 'grad-evals/s over 256 uneven posteriors in one sampler (sum of min-ESS/s beside)'
 
 
 def make_data(w):
@@ -226,20 +227,8 @@ def cpu_baseline_run(w, X, y, init, max_seconds, steps_cap, state=None, step_siz
   """Time the oracle (CPU restatement, float32, all host threads)."""
   from oracle import mcmc as omcmc
   from oracle import philox
-  from oracle import targets as ot
 
-  Xf = X.astype(np.float32)
-  yf = y.astype(np.float32)
-
-  def target(q):
-    q = q.astype(np.float32)
-    z = q @ Xf.T                                   # [C, N]
-    sp = np.logaddexp(np.float32(0), z)            # softplus(z)
-    lp = (yf * z - sp).sum(-1, dtype=np.float64)   # bernoulli.py:126-140
-    lp += (-0.5 * q.astype(np.float64) ** 2 - 0.5 * np.log(2 * np.pi)).sum(-1)
-    r = yf - np.exp(z - sp)                        # y - sigmoid(z)
-    return lp, (r @ Xf - q).astype(np.float32)
-
+  target = _logreg_f32(X, y)
   q = init.copy() if state is None else state.copy()
   lp, g = target(q)
   da = omcmc.DualAveraging(w['step0'] if step_size is None else step_size,
@@ -260,25 +249,110 @@ def cpu_baseline_run(w, X, y, init, max_seconds, steps_cap, state=None, step_siz
   return evals / dt, steps, dt
 
 
+def _logreg_f32(X, y):
+  """The oracle's logistic-regression log-density + gradient in float32 (the
+  reference's state type) with an N(0, 1) prior, for the timed CPU legs."""
+  Xf = X.astype(np.float32)
+  yf = y.astype(np.float32)
+
+  def target(q):
+    q = q.astype(np.float32)
+    z = q @ Xf.T                                   # [C, N]
+    sp = np.logaddexp(np.float32(0), z)            # softplus(z)
+    lp = (yf * z - sp).sum(-1, dtype=np.float64)   # bernoulli.py:126-140
+    lp += (-0.5 * q.astype(np.float64) ** 2 - 0.5 * np.log(2 * np.pi)).sum(-1)
+    r = yf - np.exp(z - sp)                        # y - sigmoid(z)
+    return lp, (r @ Xf - q).astype(np.float32)
+  return target
+
+
+def cpu_hmc_run(w, X, y, init, max_seconds, steps_cap):
+  """Time the oracle's HMC + Metropolis-Hastings transition (hmc.py:661-875,
+  metropolis_hastings.py:160-254; float32, all host threads) on every chain."""
+  from oracle import mcmc as omcmc
+  from oracle import philox
+  target = _logreg_f32(X, y)
+  q = init.copy()
+  lp, g = target(q)
+  evals, steps = 0, 0
+  t0 = time.perf_counter()
+  while steps < steps_cap:
+    r = omcmc.hmc_one_step(target, q, lp, g, np.float32(w['step0']), w['leapfrogs'],
+                           philox.PhiloxDraws(philox.step_key((w['seed'], 0), steps)),
+                           dtype=np.float32)
+    q, lp, g = r.next_state, r.target_log_prob, r.grads_target_log_prob
+    evals += q.shape[0] * w['leapfrogs']
+    steps += 1
+    if time.perf_counter() - t0 > max_seconds:
+      break
+  dt = time.perf_counter() - t0
+  return evals / dt, steps, dt
+
+
 def run_reference(args, w):
+  """--impl reference: the CPU restatement of the reference algorithms (the
+  oracle; TensorFlow Probability itself cannot be installed here) on the host
+  cores, for the workload, metric and unit of the engine's line."""
   world, rank, _ = dist_setup(args)
   if rank != 0:
     return
-  X, y, init = make_data(w)
   budget = float(os.environ.get('GBM_REFERENCE_SECONDS', '150'))
-  rate, steps, dt = cpu_baseline_run(w, X, y, init, budget, args.steps + args.warmup)
   cores = os.cpu_count()
+  par = 'single' if world == 1 else 'rank 0 only (host cores)'
+  if args.workload.startswith('serve_'):
+    print(json.dumps({'impl': 'reference', 'unavailable':
+                      'the serving workload measures a job server over a request stream; the '
+                      'reference has no server (its per-job sampler cost is the nuts_logreg '
+                      'reference arm)'}), flush=True)
+    return
+  if args.workload.startswith('nuts_batch'):
+    spec = make_batch_members(w)
+    rate, passes, dt, pick = cpu_batch_gradient_rate(spec, min(budget, 60.0))
+    metric, steps = METRIC_BATCH, passes
+    config = {'workload': args.workload, 'posteriors': len(spec),
+              'max_tree_depth': w['depth'], 'precision': 'f64 (NumPy oracle targets)',
+              'parallelism': par}
+    sample = ('%d passes of the log-prob+gradient of %d of the %d posteriors with all their '
+              'chains (%.1f s; the NUTS leaf cost, no tree bookkeeping); NumPy float64 oracle '
+              'targets, BLAS threads = %d' % (passes, len(pick), len(spec), dt, cores))
+  elif args.workload.startswith('hmc_'):
+    X, y, init = make_data(w)
+    rate, steps, dt = cpu_hmc_run(w, X, y, init, budget, max(1, args.steps + args.warmup))
+    metric = METRIC_HMC
+    config = {'workload': args.workload, 'rows': w['n'], 'features': w['d'],
+              'chains': w['chains'], 'step_size': w['step0'],
+              'num_leapfrog_steps': w['leapfrogs'], 'precision': 'fp32 (NumPy oracle)',
+              'parallelism': par}
+    sample = ('%d HMC transitions of all %d chains from the initial state (%.1f s); NumPy '
+              'float32 oracle, BLAS threads = %d' % (steps, w['chains'], dt, cores))
+  else:
+    X, y, init = make_data(w)
+    metric = METRIC
+    config = {'workload': args.workload, 'rows': w['n'], 'features': w['d'],
+              'chains': w['chains'], 'max_tree_depth': w['depth'],
+              'target_accept_prob': w.get('target_accept'),
+              'num_adaptation_steps': w.get('num_adaptation_steps'),
+              'precision': 'fp32 (NumPy oracle)', 'parallelism': par}
+    if w['n'] * w['d'] > 5e7:
+      # One CPU transition of this size would take hours: time the NUTS leaf
+      # cost (batched log-prob + gradient) of a 64-chain sample instead.
+      sub = min(64, w['chains'])
+      rate, steps, dt = cpu_gradient_rate(X, y, init[:sub], min(budget, 60.0))
+      sample = ('%d batched log-prob+gradient evaluations of %d of the %d chains (%.1f s; the '
+                'NUTS leaf cost, no tree bookkeeping); NumPy float32, BLAS threads = %d'
+                % (steps, sub, w['chains'], dt, cores))
+    else:
+      rate, steps, dt = cpu_baseline_run(w, X, y, init, budget, args.steps + args.warmup)
+      sample = ('%d DA(NUTS) transitions of all %d chains from the initial state, NumPy '
+                'float32 oracle, BLAS threads = %d, stopped after %.0f s'
+                % (steps, w['chains'], cores, budget))
   line = {
-      'impl': 'reference', 'metric': METRIC, 'value': rate, 'unit': 'grad-evals/s',
+      'impl': 'reference', 'metric': metric, 'value': rate, 'unit': 'grad-evals/s',
       'n_gpus': args.gpus, 'steps': steps, 'warmup': 0, 'ms_per_step': 1000 * dt / max(steps, 1),
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-      'data': 'synthetic (seeded numpy)',
-      'config': {'workload': args.workload, 'chains': w['chains'], 'rows': w['n'],
-                 'features': w['d'], 'max_tree_depth': w['depth'], 'parallelism': 'replicas'},
+      'data': 'synthetic (seeded numpy)', 'config': config,
       'cpu_baseline': {'value': rate, 'unit': 'grad-evals/s', 'cores': cores, 'kind': 'port',
-                       'sample': '%d DA(NUTS) transitions of all %d chains from the initial '
-                                 'state, NumPy float32 oracle, BLAS threads = %d, stopped after '
-                                 '%.0f s' % (steps, w['chains'], cores, budget)},
+                       'sample': sample},
       'e2e': {'value': rate, 'unit': 'grad-evals/s', 'h2d_bytes_per_step': 0,
               'd2h_bytes_per_step': 0},
   }
@@ -792,7 +866,7 @@ def run_batch(args, w):
                      'their chains (%.1f s; the NUTS leaf cost, no tree bookkeeping); NumPy '
                      'float64 oracle targets, BLAS threads = all cores' % (passes, dt)}
   line = {
-      'metric': 'grad-evals/s over 256 uneven posteriors in one sampler (sum of min-ESS/s beside)',
+      'metric': METRIC_BATCH,
       'value': grad_evals / secs, 'unit': 'grad-evals/s', 'n_gpus': 1, 'steps': args.steps,
       'warmup': args.warmup, 'ms_per_step': step_ms / args.steps, 'higher_is_better': True,
       'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32 (f64 energies)',
