@@ -141,7 +141,6 @@ def test_nuts_reproducible(pg):
 
 def test_dual_averaging_golden_constants_on_device(pg):
   # dual_averaging_step_size_adaptation_test.py:47-57 through the C ABI.
-  import ctypes
   from probability_gb300 import _native
   for err, expected in [(-0.05, 9.131008), (-0.02, 9.642897), (-0.01, 9.819825), (0.0, 10.0),
                         (0.01, 10.183481)]:

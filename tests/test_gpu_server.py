@@ -83,7 +83,6 @@ def test_server_result_is_the_same_alone_and_in_the_mix(pg):
 
 def test_server_admission_respects_budget(pg):
   from probability_gb300.serving import Server, DONE
-  from probability_gb300 import _native
   one = _problems.logreg_data(3000, 20, seed=1)
   srv = Server(workers=4, memory_budget_bytes=1)
   with pytest.raises(MemoryError):
