@@ -16,7 +16,8 @@ API with the state, log-density and gradients copied in from pinned host
 memory and the next state and accept ratios copied back every step.
 
 ``--impl reference`` times the CPU restatement of the reference algorithm
-(the oracle, NumPy float32, all host threads) on the same workload.
+(the oracle's samplers in NumPy, the float32 logistic-regression target on
+torch CPU ops, all host threads) on the same workload.
 """
 import argparse
 import json
@@ -91,22 +92,17 @@ def engine_features(X, w):
 
 
 def cpu_gradient_rate(X, y, q, max_seconds):
-  """grad-evals/s of the oracle's batched log-density + gradient (NumPy float32,
-  all host threads) on the chains of `q`: the per-leaf cost of NUTS, for
-  workloads where one CPU transition would take minutes."""
-  Xf = X.astype(np.float32)
-  yf = y.astype(np.float32)
+  """grad-evals/s of the batched log-density + gradient (float32, all host
+  threads, see _logreg_f32) on the chains of `q`: the per-leaf cost of NUTS,
+  for workloads where one CPU transition would take minutes."""
+  target = _logreg_f32(X, y)
   evals = 0
   t0 = time.perf_counter()
   while True:
-    z = q @ Xf.T
-    sp = np.logaddexp(np.float32(0), z)
-    lp = (yf * z - sp).sum(-1, dtype=np.float64)
-    g = (yf - np.exp(z - sp)) @ Xf - q
+    target(q)
     evals += q.shape[0]
     if time.perf_counter() - t0 > max_seconds:
       break
-  del lp, g
   dt = time.perf_counter() - t0
   return evals / dt, evals // q.shape[0], dt
 
@@ -251,18 +247,25 @@ def cpu_baseline_run(w, X, y, init, max_seconds, steps_cap, state=None, step_siz
 
 def _logreg_f32(X, y):
   """The oracle's logistic-regression log-density + gradient in float32 (the
-  reference's state type) with an N(0, 1) prior, for the timed CPU legs."""
-  Xf = X.astype(np.float32)
-  yf = y.astype(np.float32)
+  reference's state type) with an N(0, 1) prior, for the timed CPU legs.
+  Evaluated with torch CPU ops on all host threads: the [chains, rows]
+  elementwise passes (softplus, sigmoid) dominate, and NumPy runs them on one
+  thread, where the reference's compiled CPU path would fuse and parallelise
+  them (5-6x slower at 1e5 x 100 x 1024 on 8 cores)."""
+  import torch
+  torch.set_num_threads(os.cpu_count() or 1)
+  Xt = torch.from_numpy(np.ascontiguousarray(X, dtype=np.float32))
+  yt = torch.from_numpy(np.ascontiguousarray(y, dtype=np.float32))
+  half_log_2pi = 0.5 * np.log(2 * np.pi)
 
   def target(q):
-    q = q.astype(np.float32)
-    z = q @ Xf.T                                   # [C, N]
-    sp = np.logaddexp(np.float32(0), z)            # softplus(z)
-    lp = (yf * z - sp).sum(-1, dtype=np.float64)   # bernoulli.py:126-140
-    lp += (-0.5 * q.astype(np.float64) ** 2 - 0.5 * np.log(2 * np.pi)).sum(-1)
-    r = yf - np.exp(z - sp)                        # y - sigmoid(z)
-    return lp, (r @ Xf - q).astype(np.float32)
+    qt = torch.from_numpy(np.ascontiguousarray(q, dtype=np.float32))
+    z = qt @ Xt.T                                                # [C, N]
+    sp = torch.nn.functional.softplus(z)
+    lp = (yt * z - sp).sum(-1, dtype=torch.float64)              # bernoulli.py:126-140
+    lp += (-0.5 * qt.double() ** 2 - half_log_2pi).sum(-1)
+    g = (yt - torch.sigmoid(z)) @ Xt - qt
+    return lp.numpy(), g.numpy()
   return target
 
 
@@ -323,8 +326,9 @@ def run_reference(args, w):
               'chains': w['chains'], 'step_size': w['step0'],
               'num_leapfrog_steps': w['leapfrogs'], 'precision': 'fp32 (NumPy oracle)',
               'parallelism': par}
-    sample = ('%d HMC transitions of all %d chains from the initial state (%.1f s); NumPy '
-              'float32 oracle, BLAS threads = %d' % (steps, w['chains'], dt, cores))
+    sample = ('%d HMC transitions of all %d chains from the initial state (%.1f s); oracle '
+              'HMC in NumPy, float32 target on torch CPU ops, %d threads'
+              % (steps, w['chains'], dt, cores))
   else:
     X, y, init = make_data(w)
     metric = METRIC
@@ -339,13 +343,13 @@ def run_reference(args, w):
       sub = min(64, w['chains'])
       rate, steps, dt = cpu_gradient_rate(X, y, init[:sub], min(budget, 60.0))
       sample = ('%d batched log-prob+gradient evaluations of %d of the %d chains (%.1f s; the '
-                'NUTS leaf cost, no tree bookkeeping); NumPy float32, BLAS threads = %d'
+                'NUTS leaf cost, no tree bookkeeping); float32 torch CPU ops, %d threads'
                 % (steps, sub, w['chains'], dt, cores))
     else:
       rate, steps, dt = cpu_baseline_run(w, X, y, init, budget, args.steps + args.warmup)
-      sample = ('%d DA(NUTS) transitions of all %d chains from the initial state, NumPy '
-                'float32 oracle, BLAS threads = %d, stopped after %.0f s'
-                % (steps, w['chains'], cores, budget))
+      sample = ('%d DA(NUTS) transitions of all %d chains from the initial state; oracle '
+                'NUTS in NumPy, float32 target on torch CPU ops, %d threads; stopped after '
+                '%.0f s' % (steps, w['chains'], cores, budget))
   line = {
       'impl': 'reference', 'metric': metric, 'value': rate, 'unit': 'grad-evals/s',
       'n_gpus': args.gpus, 'steps': steps, 'warmup': 0, 'ms_per_step': 1000 * dt / max(steps, 1),
@@ -635,8 +639,8 @@ def run_engine(args, w):
     rate, nev, dt = cpu_gradient_rate(X, y, state[:sub].cpu().numpy(), budget)
     cpu = {'value': rate, 'unit': 'grad-evals/s', 'cores': os.cpu_count(), 'kind': 'port',
            'sample': '%d batched log-prob+gradient evaluations of %d of the %d chains '
-                     '(%.1f s; the NUTS leaf cost, no tree bookkeeping); NumPy float32, '
-                     'BLAS threads = all cores' % (nev, sub, w['chains'], dt)}
+                     '(%.1f s; the NUTS leaf cost, no tree bookkeeping); float32 torch '
+                     'CPU ops, all host threads' % (nev, sub, w['chains'], dt)}
   elif rank == 0 and world == 1 and not args.no_cpu_baseline:
     budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '20'))
     sub = 64
@@ -645,8 +649,9 @@ def run_engine(args, w):
                                         step_size=float(kr.new_step_size.reshape(-1)[0].item()))
     cpu = {'value': rate, 'unit': 'grad-evals/s', 'cores': os.cpu_count(), 'kind': 'port',
            'sample': '%d DA(NUTS) transitions of %d of the %d chains, started from the '
-                     'engine\'s adapted state and step size (%.1f s); NumPy float32 oracle, '
-                     'chains in lock-step as in the reference, BLAS threads = all cores'
+                     'engine\'s adapted state and step size (%.1f s); oracle NUTS in NumPy '
+                     '(chains in lock-step as in the reference), float32 target on torch CPU '
+                     'ops, all host threads'
                      % (nsteps, sub, w['chains'], dt)}
 
   prec = None
