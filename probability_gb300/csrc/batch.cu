@@ -378,7 +378,7 @@ class BatchTarget final : public Target {
   const int* ragged_dims() const override { return cdim_.as<int>(); }
   int64_t ragged_chains() const override { return C_; }
   int64_t ragged_elements() const override { return E_; }
-  int launches_per_eval() const override { return 3; }
+  int launches_per_eval(int64_t) const override { return 3; }
 
   // All chains (the direct log_prob_and_grad call): q, grad ragged.
   void eval(const float* q, int, const int*, int, double* logp, float* grad, int, void*,

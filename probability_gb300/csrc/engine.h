@@ -78,8 +78,8 @@ struct Target {
   // Algorithmic flops and HBM bytes for one batched evaluation of n states.
   virtual double flops(int64_t n) const = 0;
   virtual double bytes(int64_t n) const = 0;
-  // Kernels one eval() launches (for launch accounting).
-  virtual int launches_per_eval() const = 0;
+  // Kernels one eval() of up to `cap` states launches (launch accounting).
+  virtual int launches_per_eval(int64_t cap) const = 0;
   // Ragged batches of posteriors (many targets of different dimension in one
   // sampler): per-chain element offsets and dimensions on the device, the
   // number of chains and the sum of their dimensions.  Uniform targets

@@ -45,9 +45,10 @@ template <int KD>
 __global__ void __launch_bounds__(kThreads)
 logreg_partial_kernel(const float* __restrict__ X, int ldx, const float* __restrict__ y, int N,
                       int D, const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev,
-                      int grid, double* __restrict__ lpart, float* __restrict__ gpart) {
+                      int c_base, int c_lim, int grid, double* __restrict__ lpart,
+                      float* __restrict__ gpart) {
   extern __shared__ __align__(16) float smem[];
-  const int n = *n_dev;
+  const int n = chunk_count(*n_dev, c_base, c_lim);
   const int row_tiles = (N + kNT - 1) / kNT;
   const int S = num_splits(n, grid, row_tiles);
   const int tiles = (n + kCT - 1) / kCT;
@@ -225,28 +226,41 @@ class LogregSimt final : public Target {
     return rows * sizeof(double) + rows * (size_t)D_ * sizeof(float) + 256;
   }
 
+  // One launch covers at most grid_ * kCT chains (one work item per CTA);
+  // larger batches run as consecutive chunks that share the workspace.
   void eval(const float* q, int ldq, const int* n_dev, int cap, double* logp, float* grad,
             int ldg, void* ws, cudaStream_t s) override {
     const size_t rows = (size_t)grid_ * kCT + (size_t)cap;
     double* lpart = static_cast<double*>(ws);
     float* gpart = reinterpret_cast<float*>(lpart + rows);
     const int N = (int)N_, D = (int)D_;
-    switch (kd_) {
-      case 2: logreg_partial_kernel<2><<<grid_, kThreads, smem_, s>>>(
-          x_.as<float>(), ldx_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart); break;
-      case 4: logreg_partial_kernel<4><<<grid_, kThreads, smem_, s>>>(
-          x_.as<float>(), ldx_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart); break;
-      case 8: logreg_partial_kernel<8><<<grid_, kThreads, smem_, s>>>(
-          x_.as<float>(), ldx_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart); break;
-      default: logreg_partial_kernel<16><<<grid_, kThreads, smem_, s>>>(
-          x_.as<float>(), ldx_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart); break;
+    const int lim = grid_ * kCT;
+    for (int base = 0; base < cap; base += lim) {
+      const float* qc = q + (size_t)base * ldq;
+      switch (kd_) {
+        case 2: logreg_partial_kernel<2><<<grid_, kThreads, smem_, s>>>(
+            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart,
+            gpart); break;
+        case 4: logreg_partial_kernel<4><<<grid_, kThreads, smem_, s>>>(
+            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart,
+            gpart); break;
+        case 8: logreg_partial_kernel<8><<<grid_, kThreads, smem_, s>>>(
+            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart,
+            gpart); break;
+        default: logreg_partial_kernel<16><<<grid_, kThreads, smem_, s>>>(
+            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart,
+            gpart); break;
+      }
+      GBM_CUDA(cudaGetLastError());
+      launch_split_reduce(lpart, gpart, qc, ldq, n_dev, base, lim, std::min(lim, cap - base),
+                          kCT, kNT, grid_, N, D, inv_var_, log_norm_, nullptr, logp + base,
+                          grad + (size_t)base * ldg, ldg, s);
     }
-    GBM_CUDA(cudaGetLastError());
-    launch_split_reduce(lpart, gpart, q, ldq, n_dev, cap, kCT, kNT, grid_, N, D, inv_var_,
-                        log_norm_, nullptr, logp, grad, ldg, s);
   }
 
-  int launches_per_eval() const override { return 2; }
+  int launches_per_eval(int64_t cap) const override {
+    return 2 * (int)((cap + (int64_t)grid_ * kCT - 1) / ((int64_t)grid_ * kCT));
+  }
   double flops(int64_t n) const override { return 4.0 * (double)N_ * D_ * n; }
   double bytes(int64_t n) const override {
     return 4.0 * (double)N_ * D_ + 4.0 * N_ + 8.0 * (double)n * D_ + 8.0 * n;
@@ -321,8 +335,11 @@ std::vector<NoAllocDevice> g_noalloc_devices;
 
 // Once per device, with that device current: resolve the device address of
 // the scratch array (its host-side name is only a stand-in) and raise the
-// kernels' dynamic shared-memory limit.  Allocates nothing.
-int noalloc_setup(int device, NoAllocDevice** out) {
+// kernels' dynamic shared-memory limit.  Allocates nothing on the device.
+// The record is copied out while the lock is held: a first call on a
+// higher-numbered device from another thread may grow the vector and move
+// its elements.
+int noalloc_setup(int device, NoAllocDevice* out) {
   std::lock_guard<std::mutex> lock(g_noalloc_mu);
   if ((int)g_noalloc_devices.size() <= device) g_noalloc_devices.resize(device + 1);
   NoAllocDevice& d = g_noalloc_devices[device];
@@ -356,7 +373,7 @@ int noalloc_setup(int device, NoAllocDevice** out) {
     d.scratch = static_cast<unsigned char*>(p);
     d.ready = true;
   }
-  *out = &d;
+  *out = d;
   return GBM_OK;
 }
 
@@ -389,7 +406,7 @@ extern "C" int gbm_logreg_log_prob_and_grad_noalloc(const float* x, int64_t num_
     gbm::set_error(std::string("cudaGetDevice: ") + cudaGetErrorString(e));
     return GBM_ECUDA;
   }
-  NoAllocDevice* dev = nullptr;
+  NoAllocDevice dev;
   int st = noalloc_setup(device, &dev);
   if (st != GBM_OK) return st;
 
@@ -399,7 +416,7 @@ extern "C" int gbm_logreg_log_prob_and_grad_noalloc(const float* x, int64_t num_
   const int D = (int)num_features, N = (int)num_rows;
   const size_t per_row = sizeof(double) + sizeof(float) * (size_t)D;
   const size_t avail = kNoAllocScratchBytes - kNoAllocCountBytes;
-  int grid = 2 * dev->num_sms;
+  int grid = 2 * dev.num_sms;
   const int fit = (int)(avail / (per_row * gbm::kCT));
   grid = std::min(grid, fit);
   if (grid < 1 || chains > (int64_t)grid * gbm::kCT) {
@@ -412,8 +429,8 @@ extern "C" int gbm_logreg_log_prob_and_grad_noalloc(const float* x, int64_t num_
     return GBM_EINVAL;
   }
   const int n = (int)chains;
-  int* count = reinterpret_cast<int*>(dev->scratch);
-  double* lpart = reinterpret_cast<double*>(dev->scratch + kNoAllocCountBytes);
+  int* count = reinterpret_cast<int*>(dev.scratch);
+  double* lpart = reinterpret_cast<double*>(dev.scratch + kNoAllocCountBytes);
   float* gpart = reinterpret_cast<float*>(lpart + (size_t)grid * gbm::kCT);
   cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
   const int kd = D <= 32 ? 2 : D <= 64 ? 4 : D <= 128 ? 8 : 16;
@@ -424,13 +441,13 @@ extern "C" int gbm_logreg_log_prob_and_grad_noalloc(const float* x, int64_t num_
   noalloc_set_count<<<1, 1, 0, s>>>(count, n);
   switch (kd) {
     case 2: gbm::logreg_partial_kernel<2><<<grid, gbm::kThreads, smem, s>>>(
-        x, D, y, N, D, state, D, count, grid, lpart, gpart); break;
+        x, D, y, N, D, state, D, count, 0, grid * gbm::kCT, grid, lpart, gpart); break;
     case 4: gbm::logreg_partial_kernel<4><<<grid, gbm::kThreads, smem, s>>>(
-        x, D, y, N, D, state, D, count, grid, lpart, gpart); break;
+        x, D, y, N, D, state, D, count, 0, grid * gbm::kCT, grid, lpart, gpart); break;
     case 8: gbm::logreg_partial_kernel<8><<<grid, gbm::kThreads, smem, s>>>(
-        x, D, y, N, D, state, D, count, grid, lpart, gpart); break;
+        x, D, y, N, D, state, D, count, 0, grid * gbm::kCT, grid, lpart, gpart); break;
     default: gbm::logreg_partial_kernel<16><<<grid, gbm::kThreads, smem, s>>>(
-        x, D, y, N, D, state, D, count, grid, lpart, gpart); break;
+        x, D, y, N, D, state, D, count, 0, grid * gbm::kCT, grid, lpart, gpart); break;
   }
   gbm::logreg_reduce_kernel<<<(n + 7) / 8, 256, 0, s>>>(lpart, gpart, state, D, count, grid, N,
                                                          D, inv_var, log_norm, log_prob, grad, D);

@@ -146,8 +146,8 @@ __global__ void __launch_bounds__(tc_threads(EPI), 1)
 logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
                  const __grid_constant__ CUtensorMap xlomap, const float* __restrict__ y, int N,
                  int D, const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev,
-                 int grid, double* __restrict__ lpart, float* __restrict__ gpart,
-                 int* __restrict__ err) {
+                 int c_base, int c_lim, int grid, double* __restrict__ lpart,
+                 float* __restrict__ gpart, int* __restrict__ err) {
   using L = TcLayout<KB, CT, XLO>;
   constexpr int kThreads = tc_threads(EPI);
   constexpr int kCW = CT * 4 / EPI;             // chains per epilogue warp
@@ -155,7 +155,7 @@ logreg_tc_kernel(const __grid_constant__ CUtensorMap xmap,
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const int n = *n_dev;
+  const int n = chunk_count(*n_dev, c_base, c_lim);
   const int row_tiles = (N + kRows - 1) / kRows;
   const int S = tc_splits(n, CT, grid, row_tiles);
   const int tiles = (n + CT - 1) / CT;
@@ -575,15 +575,15 @@ __global__ void __launch_bounds__(tc_threads(kTctEpi), 1)
 logreg_tct_kernel(const __grid_constant__ CUtensorMap xmap,
                   const __grid_constant__ CUtensorMap xlomap, const float* __restrict__ ym,
                   int N, int D, const float* __restrict__ Q, int ldq,
-                  const int* __restrict__ n_dev, int grid, double* __restrict__ lpart,
-                  float* __restrict__ gpart, int* __restrict__ err) {
+                  const int* __restrict__ n_dev, int c_base, int c_lim, int grid,
+                  double* __restrict__ lpart, float* __restrict__ gpart, int* __restrict__ err) {
   using L = TctLayout<XLO>;
   constexpr int CT = 128;
   constexpr int kThreads = tc_threads(kTctEpi);
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const int n = *n_dev;
+  const int n = chunk_count(*n_dev, c_base, c_lim);
   const int row_tiles = (N + kRows - 1) / kRows;
   const int S = tc_splits(n, CT, grid, row_tiles);
   const int tiles = (n + CT - 1) / CT;
@@ -904,14 +904,15 @@ __device__ __forceinline__ bool wait_cluster_or_abort(uint64_t* bar, uint32_t pa
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(tc_threads(kPairEpi), 1)
 logreg_tc_pair_kernel(const __grid_constant__ CUtensorMap xmap, const float* __restrict__ y,
                       int N, int D, const float* __restrict__ Q, int ldq,
-                      const int* __restrict__ n_dev, int pairs, double* __restrict__ lpart,
-                      float* __restrict__ gpart, int* __restrict__ err) {
+                      const int* __restrict__ n_dev, int c_base, int c_lim, int pairs,
+                      double* __restrict__ lpart, float* __restrict__ gpart,
+                      int* __restrict__ err) {
   using L = PairLayout;
   constexpr int CT = kPairCT;
   extern __shared__ __align__(1024) unsigned char smem_raw[];
   unsigned char* smem = reinterpret_cast<unsigned char*>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
-  const int n = *n_dev;
+  const int n = chunk_count(*n_dev, c_base, c_lim);
   const int row_tiles = (N + kRows - 1) / kRows;
   const int S = tc_splits(n, CT, pairs, row_tiles);
   const int tiles = (n + CT - 1) / CT;
@@ -1422,26 +1423,38 @@ class LogregTc final : public Target {
     double* lpart = static_cast<double*>(ws);
     float* gpart = reinterpret_cast<float*>(lpart + rows);
     const int N = (int)N_, D = (int)D_;
+    // One launch covers at most grid_ * ct_ chains (one work item per CTA or
+    // CTA pair); larger batches run as consecutive chunks sharing `ws`.
+    const int lim = grid_ * ct_;
+    for (int base = 0; base < cap; base += lim) {
+      const float* qc = q + (size_t)base * ldq;
 #define GBM_TC_LAUNCH(KB_, CT_, EPI_, XLO_)                                               \
   logreg_tc_kernel<KB_, CT_, EPI_, XLO_><<<grid_, tc_threads(EPI_), smem_, s>>>(          \
-      xmap_, xlomap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_dev_)
+      xmap_, xlomap_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart, gpart, \
+      err_dev_)
 #define GBM_TCT_LAUNCH(XLO_)                                                              \
   logreg_tct_kernel<XLO_><<<grid_, tc_threads(kTctEpi), smem_, s>>>(                       \
-      xmap_, xlomap_, ym_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_dev_)
-    if (kb_ == 2 && xlo_) GBM_TCT_LAUNCH(true);
-    else if (kb_ == 2) GBM_TCT_LAUNCH(false);
-    else if (kb_ == 4) GBM_TC_LAUNCH(4, 64, 8, false);
-    else
-      logreg_tc_pair_kernel<<<2 * grid_, tc_threads(kPairEpi), smem_, s>>>(
-          xmap_, y_.as<float>(), N, D, q, ldq, n_dev, grid_, lpart, gpart, err_dev_);
+      xmap_, xlomap_, ym_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart, gpart, \
+      err_dev_)
+      if (kb_ == 2 && xlo_) GBM_TCT_LAUNCH(true);
+      else if (kb_ == 2) GBM_TCT_LAUNCH(false);
+      else if (kb_ == 4) GBM_TC_LAUNCH(4, 64, 8, false);
+      else
+        logreg_tc_pair_kernel<<<2 * grid_, tc_threads(kPairEpi), smem_, s>>>(
+            xmap_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart, gpart,
+            err_dev_);
 #undef GBM_TC_LAUNCH
 #undef GBM_TCT_LAUNCH
-    GBM_CUDA(cudaGetLastError());
-    launch_split_reduce(lpart, gpart, q, ldq, n_dev, cap, ct_, kRows, grid_, N, D, inv_var_,
-                        log_norm_, lin_.as<double>(), logp, grad, ldg, s);
+      GBM_CUDA(cudaGetLastError());
+      launch_split_reduce(lpart, gpart, qc, ldq, n_dev, base, lim, std::min(lim, cap - base),
+                          ct_, kRows, grid_, N, D, inv_var_, log_norm_, lin_.as<double>(),
+                          logp + base, grad + (size_t)base * ldg, ldg, s);
+    }
   }
 
-  int launches_per_eval() const override { return 2; }
+  int launches_per_eval(int64_t cap) const override {
+    return 2 * (int)((cap + (int64_t)grid_ * ct_ - 1) / ((int64_t)grid_ * ct_));
+  }
   double flops(int64_t n) const override { return 4.0 * (double)N_ * D_ * n; }
   double bytes(int64_t n) const override {
     return 2.0 * (double)N_ * D_ + 4.0 * N_ + 8.0 * (double)n * D_ + 8.0 * n;

@@ -640,7 +640,7 @@ static void nuts_eval(gbm_nuts* k, cudaStream_t s, bool capturing = false) {
   const NutsDev& w = k->dev;
   if (w.ragged) {
     k->target->impl->eval_active(w.qw, w.act_idx, w.act_count, w.lw, w.gw, k->target_ws.ptr, s);
-    if (!capturing) k->prof_launches += k->target->impl->launches_per_eval();
+    if (!capturing) k->prof_launches += k->target->impl->launches_per_eval(w.C);
     return;
   }
   if (k->profiling && !capturing) {
@@ -654,7 +654,7 @@ static void nuts_eval(gbm_nuts* k, cudaStream_t s, bool capturing = false) {
     GBM_CUDA(cudaEventRecord(k->prof_events[k->prof_used], s));
   }
   k->target->impl->eval(w.qw, w.D, w.act_count, w.C, w.lw, w.gw, w.D, k->target_ws.ptr, s);
-  k->prof_launches += k->target->impl->launches_per_eval();
+  k->prof_launches += k->target->impl->launches_per_eval(w.C);
   if (k->profiling && !capturing) {
     GBM_CUDA(cudaEventRecord(k->prof_events[k->prof_used + 1], s));
     k->prof_used += 2;
@@ -755,7 +755,7 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
         GBM_CUDA(cudaGraphLaunch(it->second, s));
         ++k->graph_launches;
         k->prof_launches += (int64_t)nl * (3 + k->unrolled_leapfrog_steps * (
-            k->target->impl->launches_per_eval() + 1) - 1);
+            k->target->impl->launches_per_eval(chains) + 1) - 1);
         k->last_leaf_iterations += nl;
         leaf += nl - 1;
         continue;

@@ -23,6 +23,15 @@ namespace gbm {
 
 constexpr int kReduceWarps = 4;            // chains per CTA
 
+// Chains of one launch.  A launch covers at most grid * ct chains (one work
+// item per CTA); larger batches are evaluated as consecutive chunks of
+// `c_lim` chains starting at chain `c_base` (pointers offset by the caller).
+// Chunk k sees min(max(n - c_base, 0), c_lim) chains of the n in *n_dev.
+__host__ __device__ __forceinline__ int chunk_count(int n, int c_base, int c_lim) {
+  const int m = n - c_base;
+  return m < 0 ? 0 : (m > c_lim ? c_lim : m);
+}
+
 namespace {
 
 __device__ __forceinline__ int split_count(int n, int ct, int nt, int grid, int N) {
@@ -37,13 +46,13 @@ __device__ __forceinline__ int split_count(int n, int ct, int nt, int grid, int 
 template <int DMAX>
 __global__ void __launch_bounds__(32 * kReduceWarps)
 split_reduce_kernel(const double* __restrict__ lpart, const float* __restrict__ gpart,
-                    const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev, int ct,
-                    int nt, int grid, int N, int D, float inv_var, double log_norm,
-                    const double* __restrict__ lin, double* __restrict__ logp,
-                    float* __restrict__ grad, int ldg) {
+                    const float* __restrict__ Q, int ldq, const int* __restrict__ n_dev,
+                    int c_base, int c_lim, int ct, int nt, int grid, int N, int D,
+                    float inv_var, double log_norm, const double* __restrict__ lin,
+                    double* __restrict__ logp, float* __restrict__ grad, int ldg) {
   constexpr int kK = DMAX / 32;               // features per lane
   constexpr int U = DMAX <= 128 ? 8 : 4;      // splits in flight
-  const int n = *n_dev;
+  const int n = chunk_count(*n_dev, c_base, c_lim);
   const int c = blockIdx.x * kReduceWarps + (threadIdx.x >> 5);
   if (c >= n) return;
   const int lane = threadIdx.x & 31;
@@ -94,20 +103,25 @@ split_reduce_kernel(const double* __restrict__ lpart, const float* __restrict__ 
   if (lane == 0) logp[c] = t + (double)D * log_norm;
 }
 
+// Q, logp and grad point at chain c_base of the batch; `cap` bounds this
+// chunk's chains (<= c_lim).
 void launch_split_reduce(const double* lpart, const float* gpart, const float* Q, int ldq,
-                         const int* n_dev, int cap, int ct, int nt, int grid, int N, int D,
-                         float inv_var, double log_norm, const double* lin, double* logp,
-                         float* grad, int ldg, cudaStream_t s) {
+                         const int* n_dev, int c_base, int c_lim, int cap, int ct, int nt,
+                         int grid, int N, int D, float inv_var, double log_norm,
+                         const double* lin, double* logp, float* grad, int ldg, cudaStream_t s) {
   const unsigned blocks = (unsigned)((cap + kReduceWarps - 1) / kReduceWarps);
   if (D <= 128)
     split_reduce_kernel<128><<<blocks, 32 * kReduceWarps, 0, s>>>(
-        lpart, gpart, Q, ldq, n_dev, ct, nt, grid, N, D, inv_var, log_norm, lin, logp, grad, ldg);
+        lpart, gpart, Q, ldq, n_dev, c_base, c_lim, ct, nt, grid, N, D, inv_var, log_norm, lin,
+        logp, grad, ldg);
   else if (D <= 256)
     split_reduce_kernel<256><<<blocks, 32 * kReduceWarps, 0, s>>>(
-        lpart, gpart, Q, ldq, n_dev, ct, nt, grid, N, D, inv_var, log_norm, lin, logp, grad, ldg);
+        lpart, gpart, Q, ldq, n_dev, c_base, c_lim, ct, nt, grid, N, D, inv_var, log_norm, lin,
+        logp, grad, ldg);
   else
     split_reduce_kernel<512><<<blocks, 32 * kReduceWarps, 0, s>>>(
-        lpart, gpart, Q, ldq, n_dev, ct, nt, grid, N, D, inv_var, log_norm, lin, logp, grad, ldg);
+        lpart, gpart, Q, ldq, n_dev, c_base, c_lim, ct, nt, grid, N, D, inv_var, log_norm, lin,
+        logp, grad, ldg);
   GBM_CUDA(cudaGetLastError());
 }
 

@@ -144,7 +144,7 @@ class Mvn final : public Target {
     mvn_finish_kernel<<<(cap + 255) / 256, 256, 0, s>>>(part, dtiles_, n_dev, log_norm_, logp);
     GBM_CUDA(cudaGetLastError());
   }
-  int launches_per_eval() const override { return 3; }
+  int launches_per_eval(int64_t) const override { return 3; }
   // Two triangular GEMMs: ~D^2 multiply-adds each per chain.
   double flops(int64_t n) const override { return 2.0 * (double)dim * dim * n; }
   double bytes(int64_t n) const override {
@@ -213,7 +213,7 @@ class Hier final : public Target {
                                               logp, grad, ldg);
     GBM_CUDA(cudaGetLastError());
   }
-  int launches_per_eval() const override { return 1; }
+  int launches_per_eval(int64_t) const override { return 1; }
   double flops(int64_t n) const override { return 10.0 * (double)J_ * n; }
   double bytes(int64_t n) const override { return 8.0 * J_ + 8.0 * (double)(J_ + 2) * n + 8.0 * n; }
 

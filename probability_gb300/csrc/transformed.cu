@@ -117,7 +117,9 @@ class Transformed final : public Target {
     GBM_CUDA(cudaGetLastError());
   }
 
-  int launches_per_eval() const override { return inner_->launches_per_eval() + 2; }
+  int launches_per_eval(int64_t cap) const override {
+    return inner_->launches_per_eval(cap) + 2;
+  }
   double flops(int64_t n) const override { return inner_->flops(n) + 10.0 * (double)dim * n; }
   double bytes(int64_t n) const override { return inner_->bytes(n) + 16.0 * (double)dim * n; }
 
