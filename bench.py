@@ -33,10 +33,14 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+# step_size_draws: the step size dual averaging (target 0.8) reaches at the
+# end of the 1000-step adaptation window from the Laplace start, in FP32
+# (`bench.py --adapt`); the timed transitions are the draws that follow.
 WORKLOADS = {
     'nuts_logreg_1e5x100': dict(n=100000, d=100, chains=1024, depth=10, seed=1,
                                 feature_scale=0.1, step0=0.1, target_accept=0.8,
-                                num_adaptation_steps=1000, precision='mixed'),
+                                num_adaptation_steps=1000, precision='fp32', start='laplace',
+                                step_size_draws=0.011),
 }
 # Mixed precision at scale: X 1e6 x 512 BF16, 4096 chains, NUTS depth 8.
 WORKLOADS['nuts_logreg_1e6x512_bf16'] = dict(n=1000000, d=512, chains=4096, depth=8, seed=2,
@@ -219,30 +223,38 @@ def dist_setup(args):
   return world, rank, local
 
 
-def cpu_baseline_run(w, X, y, init, max_seconds, steps_cap, state=None, step_size=None):
-  """Time the oracle (CPU restatement, float32, all host threads)."""
+def cpu_nuts_run(w, X, y, state, eps, keys, max_seconds, timed_from=0):
+  """The oracle's DA(NUTS) transitions in the draws phase (step size `eps`,
+  adaptation over: dual averaging keeps it) on the host cores: float32 state,
+  the float32 logistic-regression target on torch CPU ops with all host
+  threads, chains in lock-step as in the reference.  Runs the transitions of
+  `keys` (the engine's draws, addressed by chain index, so chains 0..C-1 of
+  `state` follow the engine's chains 0..C-1) until `max_seconds` have
+  passed; the first `timed_from` are untimed warm-up.  Returns (useful
+  gradient evaluations per second, timed transitions, seconds)."""
   from oracle import mcmc as omcmc
   from oracle import philox
 
   target = _logreg_f32(X, y)
-  q = init.copy() if state is None else state.copy()
+  q = np.array(state, np.float32)
   lp, g = target(q)
-  da = omcmc.DualAveraging(w['step0'] if step_size is None else step_size,
-                           w['num_adaptation_steps'], w['target_accept'])
-  evals, steps = 0, 0
-  t0 = time.perf_counter()
-  while steps < steps_cap:
+  da = omcmc.DualAveraging(eps, w['num_adaptation_steps'], w['target_accept'])
+  da.step = w['num_adaptation_steps']                 # adaptation window over
+  da.log_averaging_step = np.log(np.float64(eps))
+  evals, steps, dt = 0, 0, 0.0
+  for i, key in enumerate(keys):
+    t0 = time.perf_counter()
     r = omcmc.nuts_one_step(target, q, lp, g, np.float32(da.new_step_size),
-                            philox.PhiloxDraws(philox.step_key((w['seed'], 0), steps)),
-                            w['depth'], dtype=np.float32)
+                            philox.PhiloxDraws(key), w['depth'], dtype=np.float32)
     q, lp, g = r.next_state, r.target_log_prob, r.grads_target_log_prob
     da.update(r.log_accept_ratio)
-    evals += int(r.leapfrogs_taken.sum())
-    steps += 1
-    if time.perf_counter() - t0 > max_seconds:
-      break
-  dt = time.perf_counter() - t0
-  return evals / dt, steps, dt
+    if i >= timed_from:
+      dt += time.perf_counter() - t0
+      evals += int(r.leapfrogs_taken.sum())
+      steps += 1
+      if dt > max_seconds:    # the timed budget ends the run (at least one step)
+        break
+  return evals / max(dt, 1e-9), steps, dt
 
 
 def _logreg_f32(X, y):
@@ -269,27 +281,31 @@ def _logreg_f32(X, y):
   return target
 
 
-def cpu_hmc_run(w, X, y, init, max_seconds, steps_cap):
+def cpu_hmc_run(w, X, y, init, max_seconds, warmup, steps):
   """Time the oracle's HMC + Metropolis-Hastings transition (hmc.py:661-875,
-  metropolis_hastings.py:160-254; float32, all host threads) on every chain."""
+  metropolis_hastings.py:160-254; float32, all host threads) on every chain:
+  `warmup` untimed transitions, then up to `steps` timed ones (at least one)
+  within `max_seconds`.  Transition t uses sample_chain's key t, so a
+  fixed-step HMC run costs the same per transition from any state."""
   from oracle import mcmc as omcmc
   from oracle import philox
   target = _logreg_f32(X, y)
   q = init.copy()
   lp, g = target(q)
-  evals, steps = 0, 0
-  t0 = time.perf_counter()
-  while steps < steps_cap:
+  evals, done, dt = 0, 0, 0.0
+  for t in range(warmup + steps):
+    t0 = time.perf_counter()
     r = omcmc.hmc_one_step(target, q, lp, g, np.float32(w['step0']), w['leapfrogs'],
-                           philox.PhiloxDraws(philox.step_key((w['seed'], 0), steps)),
+                           philox.PhiloxDraws(philox.step_key((w['seed'], 0), t)),
                            dtype=np.float32)
     q, lp, g = r.next_state, r.target_log_prob, r.grads_target_log_prob
-    evals += q.shape[0] * w['leapfrogs']
-    steps += 1
-    if time.perf_counter() - t0 > max_seconds:
-      break
-  dt = time.perf_counter() - t0
-  return evals / dt, steps, dt
+    if t >= warmup:
+      dt += time.perf_counter() - t0
+      evals += q.shape[0] * w['leapfrogs']
+      done += 1
+      if dt > max_seconds:
+        break
+  return evals / max(dt, 1e-9), done, dt
 
 
 def run_reference(args, w):
@@ -299,7 +315,7 @@ def run_reference(args, w):
   world, rank, _ = dist_setup(args)
   if rank != 0:
     return
-  budget = float(os.environ.get('GBM_REFERENCE_SECONDS', '150'))
+  budget = float(os.environ.get('GBM_REFERENCE_SECONDS', '300'))
   cores = os.cpu_count()
   par = 'single' if world == 1 else 'rank 0 only (host cores)'
   if args.workload.startswith('serve_'):
@@ -320,15 +336,14 @@ def run_reference(args, w):
               'targets, BLAS threads = %d' % (passes, len(pick), len(spec), dt, cores))
   elif args.workload.startswith('hmc_'):
     X, y, init = make_data(w)
-    rate, steps, dt = cpu_hmc_run(w, X, y, init, budget, max(1, args.steps + args.warmup))
+    rate, steps, dt = cpu_hmc_run(w, X, y, init, budget, args.warmup, args.steps)
     metric = METRIC_HMC
-    config = {'workload': args.workload, 'rows': w['n'], 'features': w['d'],
-              'chains': w['chains'], 'step_size': w['step0'],
-              'num_leapfrog_steps': w['leapfrogs'], 'precision': 'fp32 (NumPy oracle)',
-              'parallelism': par}
-    sample = ('%d HMC transitions of all %d chains from the initial state (%.1f s); oracle '
-              'HMC in NumPy, float32 target on torch CPU ops, %d threads'
-              % (steps, w['chains'], dt, cores))
+    config = hmc_config(args, w, 'fp32')
+    sample = ('each step: one HMC transition (10 leapfrog steps) of all %d chains, after %d '
+              'untimed warm-up transitions (a fixed-step HMC transition costs the same from '
+              'any state); oracle HMC + Metropolis-Hastings in NumPy, float32 target on torch '
+              'CPU ops, %d threads; %d of %d timed steps (%.2f s timed)'
+              % (w['chains'], args.warmup, cores, steps, args.steps, dt))
   else:
     X, y, init = make_data(w)
     metric = METRIC
@@ -346,15 +361,34 @@ def run_reference(args, w):
                 'NUTS leaf cost, no tree bookkeeping); float32 torch CPU ops, %d threads'
                 % (steps, sub, w['chains'], dt, cores))
     else:
-      rate, steps, dt = cpu_baseline_run(w, X, y, init, budget, args.steps + args.warmup)
-      sample = ('%d DA(NUTS) transitions of all %d chains from the initial state; oracle '
-                'NUTS in NumPy, float32 target on torch CPU ops, %d threads; stopped after '
-                '%.0f s' % (steps, w['chains'], cores, budget))
+      from oracle import philox
+      # The engine arm's timed transitions: same Laplace start, step size and
+      # keys (sample_chain steps num_adaptation_steps + i), all chains; the
+      # first `warmup` transitions are run untimed, as in the engine arm.
+      init = laplace_start(X, y, w['chains'], w['seed'])
+      sub = min(int(os.environ.get('GBM_REFERENCE_CHAINS', '128')), w['chains'])
+      t0 = w['num_adaptation_steps']
+      keys = [philox.step_key((w['seed'], 0), t0 + i) for i in range(args.warmup + args.steps)]
+      rate, steps, dt = cpu_nuts_run(w, X, y, init[:sub], w['step_size_draws'], keys, budget,
+                                     timed_from=args.warmup)
+      config = nuts_config(args, w, 'fp32', world)
+      sample = ('each step: one DA(NUTS) transition of chains 0-%d of the %d, in the draws '
+                'phase, from the same Laplace start, step size %g and transition keys as the '
+                'engine arm, so these chains follow the engine\'s chains 0-%d (same draws); %d '
+                'untimed warm-up transitions first; oracle NUTS in NumPy (chains in lock-step), '
+                'float32 target on torch CPU ops, %d threads; %d of %d timed steps within the '
+                '%.0f s budget (%.1f s timed)'
+                % (sub - 1, w['chains'], w['step_size_draws'], sub - 1, args.warmup, cores,
+                   steps, args.steps, budget, dt))
   line = {
       'impl': 'reference', 'metric': metric, 'value': rate, 'unit': 'grad-evals/s',
-      'n_gpus': args.gpus, 'steps': steps, 'warmup': 0, 'ms_per_step': 1000 * dt / max(steps, 1),
+      'n_gpus': args.gpus, 'steps': steps,
+      'warmup': args.warmup if (w.get('start') == 'laplace' or
+                                args.workload.startswith('hmc_')) else 0,
+      'ms_per_step': 1000 * dt / max(steps, 1),
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
-      'data': 'synthetic (seeded numpy)', 'config': config,
+      'data': ('synthetic (seeded numpy default_rng(%d))' % w['seed']) if 'seed' in w
+              else 'synthetic (seeded numpy)', 'config': config,
       'cpu_baseline': {'value': rate, 'unit': 'grad-evals/s', 'cores': cores, 'kind': 'port',
                        'sample': sample},
       'e2e': {'value': rate, 'unit': 'grad-evals/s', 'h2d_bytes_per_step': 0,
@@ -389,14 +423,23 @@ def run_kernel_only(args, w):
                     'tflops': flops / ms / 1e9, 'chains': q.shape[0]}), flush=True)
 
 
+def hmc_config(args, w, precision):
+  return {'workload': args.workload, 'rows': w['n'], 'features': w['d'],
+          'chains': w['chains'], 'step_size': w['step0'],
+          'num_leapfrog_steps': w['leapfrogs'], 'burnin': w['burnin'],
+          'precision': precision, 'l2': 'inputs L2-resident (100 KB of X)',
+          'parallelism': 'single'}
+
+
 def run_hmc(args, w):
   """HMC on the 1000 x 25 logistic regression (64 chains, step 0.03, 10
   leapfrog steps): burn-in untimed, then K transitions timed through the
-  device-resident chain loop."""
+  device-resident chain loop (one CUDA graph per transition)."""
   import torch
   import probability_gb300 as pg
   X, y, init = make_data(w)
-  target = pg.LogisticRegression(X, y, precision=args.precision or w['precision'])
+  precision = args.precision or w['precision']
+  target = pg.LogisticRegression(X, y, precision=precision)
   k = pg.mcmc.HamiltonianMonteCarlo(target, step_size=w['step0'],
                                     num_leapfrog_steps=w['leapfrogs'])
   q = torch.from_numpy(init).cuda()
@@ -404,6 +447,8 @@ def run_hmc(args, w):
                           seed=(w['seed'], 0))
   q = run.final_state
   first = w['burnin'] + args.warmup
+  clocks = ClockSampler(torch.cuda.current_device())
+  clocks.start()
   torch.cuda.synchronize()
   e0 = torch.cuda.Event(enable_timing=True)
   e1 = torch.cuda.Event(enable_timing=True)
@@ -411,6 +456,7 @@ def run_hmc(args, w):
   run = pg.mcmc.run_chain(k, args.steps, q, seed=(w['seed'], 0), first_step=first)
   e1.record()
   e1.synchronize()
+  clk = clocks.stop()
   secs = e0.elapsed_time(e1) / 1000.0
   evals = args.steps * w['chains'] * w['leapfrogs']
   acc = run.trace['is_accepted'].float().mean().item()
@@ -422,19 +468,291 @@ def run_hmc(args, w):
   ess = pg.mcmc.effective_sample_size(ess_run.all_states, filter_beyond_positive_pairs=True,
                                       cross_chain_dims=1)
   ess_per_draw = float(ess.min().item()) / n_ess
+
+  # ---- end to end: HamiltonianMonteCarlo.one_step with host buffers ----
+  C, D = q.shape
+  h_state = torch.from_numpy(init).pin_memory()
+  kr = k.bootstrap_results(torch.from_numpy(init).cuda())
+  h_tlp = kr.accepted_results.target_log_prob.cpu().pin_memory()
+  h_grad = kr.accepted_results.grads_target_log_prob.cpu().pin_memory()
+  h_out = torch.empty((C, D), dtype=torch.float32).pin_memory()
+  h_acc = torch.empty(C, dtype=torch.bool).pin_memory()
+  for t in range(args.warmup + args.steps):
+    if t == args.warmup:
+      torch.cuda.synchronize()
+      e0.record()
+    acc_r = kr.accepted_results._replace(
+        target_log_prob=h_tlp.cuda(non_blocking=True),
+        grads_target_log_prob=h_grad.cuda(non_blocking=True))
+    s_, kr = k.one_step(h_state.cuda(non_blocking=True), kr._replace(accepted_results=acc_r),
+                        seed=pg._util.step_key((w['seed'], 0), t))
+    h_out.copy_(s_, non_blocking=True)
+    h_tlp.copy_(kr.accepted_results.target_log_prob, non_blocking=True)
+    h_grad.copy_(kr.accepted_results.grads_target_log_prob, non_blocking=True)
+    h_acc.copy_(kr.is_accepted, non_blocking=True)
+    torch.cuda.current_stream().synchronize()
+    h_state.copy_(h_out)
+  e1.record()
+  e1.synchronize()
+  e2e_s = e0.elapsed_time(e1) / 1000.0
+  e2e = {'value': evals / e2e_s, 'unit': 'grad-evals/s',
+         'h2d_bytes_per_step': C * D * 4 * 2 + C * 8, 'd2h_bytes_per_step': C * D * 8 + C * 9,
+         'steps': args.steps,
+         'transitions': 'HamiltonianMonteCarlo.one_step per transition, state, log-density and '
+                        'gradients copied in from pinned host memory and back every step'}
+
+  # ---- roofline: the batched gradient alone at the 64-chain batch ----
+  reps = 200
+  for _ in range(10):
+    target.log_prob_and_grad(q)
+  e0.record()
+  for _ in range(reps):
+    target.log_prob_and_grad(q)
+  e1.record()
+  e1.synchronize()
+  t_eval = e0.elapsed_time(e1) / 1000.0 / reps
+  flops, _ = target.cost(C)
+  peaks, _ = read_peaks()
+  sm_max = (clk or {}).get('sm_max_mhz') or peaks.get('sm_max_mhz', 2070.0)
+  peak, sms = fp32_peak_tflops(sm_max)
+  achieved = flops / t_eval / 1e12
+  roofline = {'bound': 'fp32', 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
+              'frac': achieved / peak, 'traffic': read_traffic(args.workload,
+                                                               kernel_name(precision, D)),
+              'kernel': kernel_name(precision, D),
+              'peak_source': 'nominal FP32 FMA rate: %d SMs x 128 lanes x 2 flop x %.0f MHz'
+                             % (sms, sm_max),
+              'eval_us': 1e6 * t_eval,
+              'note': 'X is 100 KB and the batch 64 chains: one evaluation is a few '
+                      'microseconds of latency (launch + one row split per CTA), far from '
+                      'any throughput roof; the bound that matters here is latency'}
+  cpu = None
+  if not args.no_cpu_baseline:
+    budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '20'))
+    rate, nsteps, dt = cpu_hmc_run(w, X, y, init, budget, args.warmup, args.steps)
+    cpu = {'value': rate, 'unit': 'grad-evals/s', 'cores': os.cpu_count(), 'kind': 'port',
+           'sample': '%d HMC transitions of all %d chains after %d untimed (%.2f s); oracle '
+                     'HMC + Metropolis-Hastings in NumPy, float32 target on torch CPU ops, '
+                     'all host threads' % (nsteps, C, args.warmup, dt)}
   print(json.dumps({
       'metric': METRIC_HMC, 'value': evals / secs, 'unit': 'grad-evals/s', 'n_gpus': 1,
       'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1000 * secs / args.steps,
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32',
       'data': 'synthetic (seeded numpy default_rng(0))',
-      'config': {'workload': 'hmc_logreg_1000x25', 'rows': w['n'], 'features': w['d'],
-                 'chains': w['chains'], 'step_size': w['step0'],
-                 'num_leapfrog_steps': w['leapfrogs'], 'burnin': w['burnin'],
-                 'precision': target.precision, 'l2': 'inputs L2-resident (100 KB of X)'},
+      'config': hmc_config(args, w, precision),
       'min_ess_per_s': ess_per_draw * args.steps / secs,
       'min_ess_note': 'min over dimensions of cross-chain ESS (diagnostic.py:203-337) of 500 '
                       'further draws, per draw, times the timed draws per second',
-      'accept_rate': acc}), flush=True)
+      'accept_rate': acc, 'e2e': e2e, 'roofline': roofline, 'cpu_baseline': cpu,
+      # per transition: momentum + half kick, L x (gradient kernel + split
+      # reduction), L - 1 kick-drift, MH finish, next step key
+      'gpu_launches': args.steps * (3 * w['leapfrogs'] + 2),
+      'clocks': clk}), flush=True)
+
+
+def laplace_start(X, y, chains, seed, prior_scale=1.0, iters=25):
+  """Chain states drawn from the posterior's Laplace approximation
+  N(beta_MAP, H^-1), H = X^T diag(s(1 - s)) X + I / prior_scale^2, with
+  beta_MAP from Newton's method (float64 NumPy, seeded): a start in the
+  typical set, shared by the engine and the reference arm, so that both time
+  transitions of the same (stationary) regime from the same state."""
+  X64 = np.asarray(X, np.float64)
+  y64 = np.asarray(y, np.float64)
+  D = X64.shape[1]
+  prec = 1.0 / prior_scale ** 2
+  beta = np.zeros(D)
+  for _ in range(iters):
+    z = X64 @ beta
+    s = 1.0 / (1.0 + np.exp(-z))
+    g = X64.T @ (y64 - s) - prec * beta
+    H = (X64 * (s * (1.0 - s))[:, None]).T @ X64 + prec * np.eye(D)
+    step = np.linalg.solve(H, g)
+    beta = beta + step
+    if np.max(np.abs(step)) < 1e-12:
+      break
+  s = 1.0 / (1.0 + np.exp(-(X64 @ beta)))
+  H = (X64 * (s * (1.0 - s))[:, None]).T @ X64 + prec * np.eye(D)
+  L = np.linalg.cholesky(H)
+  zz = np.random.default_rng(seed + 100).standard_normal((chains, D))
+  draws = beta + np.linalg.solve(L.T, zz.T).T            # cov = H^-1
+  return draws.astype(np.float32)
+
+
+def draws_phase_keys(w, count):
+  """Keys of the timed transitions: sample_chain's per-step keys (seed, 0)
+  at steps num_adaptation_steps, num_adaptation_steps + 1, ... (the first
+  draws after adaptation)."""
+  from probability_gb300 import _util
+  t0 = w['num_adaptation_steps']
+  return [_util.step_key((w['seed'], 0), t0 + i) for i in range(count)]
+
+
+def post_adaptation_results(kernel, state, eps, dev):
+  """DualAveragingStepSizeAdaptation results after its adaptation window:
+  step == num_adaptation_steps, so every later transition keeps `eps`
+  (dual_averaging_step_size_adaptation.py:468-474)."""
+  import torch
+  kr = kernel.bootstrap_results(state)
+  e = torch.full_like(kr.new_step_size, eps)
+  return kr._replace(step=int(kernel.num_adaptation_steps),
+                     log_averaging_step=torch.log(e.to(torch.float64)), new_step_size=e)
+
+
+def fp32_peak_tflops(sm_max_mhz):
+  """Nominal FP32 rate of the CUDA cores: SMs x 128 FMA lanes x 2 flop x the
+  maximum SM clock (the FP32 form's roof; MEASURED_PEAKS.json holds the HBM
+  and BF16 tensor peaks only)."""
+  import torch
+  sms = torch.cuda.get_device_properties(torch.cuda.current_device()).multi_processor_count
+  return sms * 128 * 2 * sm_max_mhz * 1e6 / 1e12, sms
+
+
+class Leg:
+  """Timed DA(NUTS) transitions of one target precision from one start."""
+
+  def __init__(self, pg, X_engine, y, w, precision, eps, dev):
+    self.pg = pg
+    self.target = pg.LogisticRegression(X_engine, y, precision=precision)
+    self.nuts = pg.mcmc.NoUTurnSampler(self.target, step_size=eps, max_tree_depth=w['depth'])
+    self.kernel = pg.mcmc.DualAveragingStepSizeAdaptation(
+        self.nuts, num_adaptation_steps=w['num_adaptation_steps'],
+        target_accept_prob=w['target_accept'])
+    self.eps, self.dev = eps, dev
+
+  def start(self, state):
+    return state.clone(), post_adaptation_results(self.kernel, state, self.eps, self.dev)
+
+  def prewarm(self, state, n, seed):
+    """Transitions from a copy of `state` with unrelated keys, discarded:
+    they capture the per-depth leaf graphs outside the timed region."""
+    q, kr = self.start(state)
+    for i in range(n):
+      q, kr = self.kernel.one_step(q, kr, seed=self.pg._util.step_key(seed, 10 ** 6 + i))
+    import torch
+    torch.cuda.synchronize()
+
+  def run(self, q, kr, keys, l2_flush=None, timed=True):
+    """Transitions with `keys`; with timed, CUDA events on the launching
+    stream bracket each one (L2 flushed outside the events)."""
+    import torch
+    step_ms, wall_s = [], []
+    lf = torch.zeros((), dtype=torch.int64, device=self.dev)
+    draws = []
+    for key in keys:
+      if l2_flush is not None:
+        l2_flush.zero_()
+      if timed:
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        w0 = time.perf_counter()
+        e0.record()
+      q, kr = self.kernel.one_step(q, kr, seed=key)
+      if timed:
+        e1.record()
+        e1.synchronize()
+        wall_s.append(time.perf_counter() - w0)
+        step_ms.append(e0.elapsed_time(e1))
+      lf += kr.inner_results.leapfrogs_taken.sum()
+      draws.append(q)
+    return q, kr, dict(step_ms=step_ms, wall_s=wall_s, lf=int(lf.item()), draws=draws)
+
+  def profiled(self, q, kr, keys):
+    """The same transitions with CUDA events around every batched gradient
+    (leaf-by-leaf launches): device time of the gradient kernels."""
+    import ctypes
+    _native = self.pg._native
+    h = self.nuts._handle
+    z = (ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64())
+    _native.check(_native.lib().gbm_nuts_read_profile(h, *map(ctypes.byref, z)))
+    _native.check(_native.lib().gbm_nuts_set_profiling(h, 1))
+    leaves = 0
+    import torch
+    lf = torch.zeros((), dtype=torch.int64, device=self.dev)
+    for key in keys:
+      q, kr = self.kernel.one_step(q, kr, seed=key)
+      leaves += int(getattr(self.nuts, 'last_leaf_iterations', 0) or 0)
+      lf += kr.inner_results.leapfrogs_taken.sum()
+    ms, ev, la = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+    _native.check(_native.lib().gbm_nuts_read_profile(h, ctypes.byref(ms), ctypes.byref(ev),
+                                                      ctypes.byref(la)))
+    _native.lib().gbm_nuts_set_profiling(h, 0)
+    return q, kr, dict(eval_ms=ms.value, evals=int(ev.value), leaves=leaves, lf=int(lf.item()))
+
+  def launches(self):
+    import ctypes
+    _native = self.pg._native
+    z = (ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64())
+    _native.check(_native.lib().gbm_nuts_read_profile(self.nuts._handle, *map(ctypes.byref, z)))
+    return int(z[2].value)
+
+
+def kernel_name(precision, d):
+  if precision == 'fp32':
+    return 'logreg_f32_kernel' if d <= 128 else 'logreg_partial_kernel'
+  return ('logreg_tc_pair_kernel' if d > 256 else 'logreg_tc_kernel' if d > 128 else
+          'logreg_tct_kernel')
+
+
+def leg_roofline(leg, prof, workload, d, sm_max_mhz, measured_over):
+  """Roofline of the dominant kernel (the batched gradient: partial kernel
+  + split reduction) from the profiled pass: algorithmic 4 N D flops per
+  useful gradient evaluation over the summed event time of the launches."""
+  flops_per_grad, _ = leg.target.cost(1)
+  eval_s = prof['eval_ms'] / 1000.0
+  achieved = flops_per_grad * prof['lf'] / eval_s / 1e12 if eval_s > 0 else None
+  name = kernel_name(leg.target.precision, d)
+  if leg.target.precision == 'fp32':
+    peak, sms = fp32_peak_tflops(sm_max_mhz)
+    bound, src = 'fp32', ('nominal FP32 FMA rate: %d SMs x 128 lanes x 2 flop x %.0f MHz '
+                          '(MEASURED_PEAKS.json has no FP32 CUDA-core peak)' % (sms, sm_max_mhz))
+  else:
+    peaks, peak_src = read_peaks()
+    peak, bound = peaks['bf16_tflops'], 'tensor'
+    src = peak_src + ' (MEASURED_PEAKS.json bf16_tflops burst)'
+  return {'bound': bound, 'achieved': achieved, 'peak': peak, 'unit': 'TFLOP/s',
+          'frac': achieved / peak if achieved else None,
+          'traffic': read_traffic(workload, name), 'kernel': name, 'peak_source': src,
+          'eval_launches': prof['evals'], 'eval_ms_total': prof['eval_ms'],
+          'alg_flops_per_grad_eval': flops_per_grad, 'measured_over': measured_over}
+
+
+def min_ess_per_s(pg, draws, secs):
+  """min over dimensions of the cross-chain ESS (diagnostic.py:220-275, with
+  filter_beyond_positive_pairs) of the timed draws, per second."""
+  import torch
+  if len(draws) < 4:
+    return None
+  ess = pg.mcmc.effective_sample_size(torch.stack(draws), filter_beyond_positive_pairs=True,
+                                      cross_chain_dims=1)
+  return float(ess.min().item()) / secs
+
+
+def split_rhat_max(pg, draws):
+  import torch
+  if len(draws) < 4:
+    return None
+  try:
+    return float(pg.mcmc.potential_scale_reduction(torch.stack(draws),
+                                                   split_chains=True).max().item())
+  except Exception:   # a diagnostic must never fail the benchmark line
+    return None
+
+
+def nuts_config(args, w, precision, world=1):
+  return {'workload': args.workload, 'rows': w['n'], 'features': w['d'],
+          'chains': w['chains'], 'max_tree_depth': w['depth'],
+          'target_accept_prob': w['target_accept'],
+          'num_adaptation_steps': w['num_adaptation_steps'],
+          'precision': precision,
+          'start': ('Laplace approximation of the posterior (seeded), step size %g: the '
+                    'draws phase after adaptation' % w['step_size_draws']
+                    if w.get('start') == 'laplace' else
+                    '%d dual-averaging warm-in transitions from N(0, 0.1^2)' % args.warm_in),
+          'timed_transitions': 'keys of sample_chain steps %d.. (after %d warm-up steps)'
+                               % (w['num_adaptation_steps'] + args.warmup, args.warmup)
+                               if w.get('start') == 'laplace' else 'after the warm-in',
+          'l2': 'flushed between timed steps (256 MB write outside the step events)',
+          'parallelism': 'single' if world == 1 else 'replicas x %d' % world}
 
 
 def run_engine(args, w):
@@ -446,152 +764,103 @@ def run_engine(args, w):
     import torch.distributed as dist
     dist.init_process_group('nccl')
   import probability_gb300 as pg
-  from probability_gb300 import _native
-
   from probability_gb300 import replicas
-  X, y, init = make_data(w)
-  if world > 1:  # independent replicas: per-rank init state and key
-    init = replicas.replica_init(init.shape, w['seed'], rank)
-  X_engine = engine_features(X, w)
-  target = pg.LogisticRegression(X_engine, y, precision=args.precision or w['precision'])
-  nuts = pg.mcmc.NoUTurnSampler(target, step_size=w['step0'], max_tree_depth=w['depth'])
-  kernel = pg.mcmc.DualAveragingStepSizeAdaptation(
-      nuts, num_adaptation_steps=w['num_adaptation_steps'],
-      target_accept_prob=w['target_accept'])
   dev = torch.device('cuda', local)
-  state = torch.from_numpy(init).to(dev)
-  kr = kernel.bootstrap_results(state)
-  seed = replicas.replica_key((w['seed'], 0), rank) if world > 1 else (w['seed'], 0)
-  t = 0
-
-  def step(state, kr, t):
-    return kernel.one_step(state, kr, seed=pg._util.step_key(seed, t))
-
-  for _ in range(args.warm_in + args.warmup):       # adaptation warm-in + warmup
-    state, kr = step(state, kr, t)
-    t += 1
-  torch.cuda.synchronize()
+  X, y, init = make_data(w)
+  laplace = w.get('start') == 'laplace'
+  if laplace:
+    init = laplace_start(X, y, w['chains'], w['seed'])
+  if world > 1:  # independent replicas: per-rank initial state
+    init = replicas.replica_init(init.shape, w['seed'], rank) if not laplace else \
+        laplace_start(X, y, w['chains'], w['seed'] + 7919 * rank)
+  X_engine = engine_features(X, w)
+  precision = args.precision or w['precision']
+  state0 = torch.from_numpy(init).to(dev)
   l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+  peaks, _ = read_peaks()
 
   def barrier():
     if dist is not None:
       dist.barrier()
     torch.cuda.synchronize()
 
-  # ---- device-resident timed region (leaf batches replayed as CUDA graphs) ----
-  import ctypes
-  ms0, ev0, la0 = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
-  _native.lib().gbm_nuts_read_profile(nuts._handle, ctypes.byref(ms0), ctypes.byref(ev0),
-                                      ctypes.byref(la0))
+  def keys_for(count, offset=0):
+    if laplace:
+      ks = draws_phase_keys(w, offset + count)[offset:]
+    else:
+      ks = [pg._util.step_key((w['seed'], 0), args.warm_in + offset + i) for i in range(count)]
+    if world > 1:
+      ks = [replicas.replica_key(k, rank) for k in ks]
+    return ks
+
+  if laplace:
+    eps = w['step_size_draws']
+    leg = Leg(pg, X_engine, y, w, precision, eps, dev)
+    leg.prewarm(state0, args.prewarm, (w['seed'], 1))
+    q, kr = leg.start(state0)
+  else:
+    # Dual-averaging warm-in from N(0, 0.1^2) (adaptation still running).
+    leg = Leg(pg, X_engine, y, w, precision, w['step0'], dev)
+    q = state0.clone()
+    kr = leg.kernel.bootstrap_results(q)
+    for i in range(args.warm_in):
+      q, kr = leg.kernel.one_step(q, kr, seed=pg._util.step_key((w['seed'], 0), i))
+    eps = float(kr.new_step_size.reshape(-1)[0].item())
+  start_q, start_kr = q.clone(), kr
+  q, kr, _ = leg.run(q, kr, keys_for(args.warmup), timed=False)
+  la0 = leg.launches()
   clocks = ClockSampler(local)
   clocks.start()
-  lf_total = torch.zeros((), dtype=torch.int64, device=dev)
-  draws = []
-  step_ms = 0.0
   barrier()
-  wall0 = time.perf_counter()
-  for _ in range(args.steps):
-    l2_flush.zero_()                                  # L2 flush outside the events
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    state, kr = step(state, kr, t)
-    e1.record()
-    t += 1
-    lf_total += kr.inner_results.leapfrogs_taken.sum()
-    draws.append(state)
-    e1.synchronize()
-    step_ms += e0.elapsed_time(e1)
+  q, kr, tm = leg.run(q, kr, keys_for(args.steps, args.warmup), l2_flush=l2_flush)
   barrier()
-  wall = time.perf_counter() - wall0
   clk = clocks.stop()
-  eval_ms, evals, launches = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
-  _native.check(_native.lib().gbm_nuts_read_profile(
-      nuts._handle, ctypes.byref(eval_ms), ctypes.byref(evals), ctypes.byref(launches)))
-  grad_evals = int(lf_total.item())
-  # ---- profiled pass of the same length: CUDA events on the launching
-  # stream bracket every batched gradient evaluation (leaf-by-leaf launches)
-  _native.check(_native.lib().gbm_nuts_set_profiling(nuts._handle, 1))
-  lf_prof = torch.zeros((), dtype=torch.int64, device=dev)
-  leaves_prof = 0          # leaf iterations (batched evaluations) of the profiled pass
-  for _ in range(args.steps):
-    state, kr = step(state, kr, t)
-    t += 1
-    leaves_prof += int(getattr(nuts, 'last_leaf_iterations', 0) or 0)
-    lf_prof += kr.inner_results.leapfrogs_taken.sum()
-  prof_ms, prof_evals, prof_la = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
-  _native.check(_native.lib().gbm_nuts_read_profile(
-      nuts._handle, ctypes.byref(prof_ms), ctypes.byref(prof_evals), ctypes.byref(prof_la)))
-  _native.lib().gbm_nuts_set_profiling(nuts._handle, 0)
-  secs = step_ms / 1000.0
-  secs, grad_evals = replicas.combine_throughput(secs, grad_evals)   # max time, total work
+  launches = leg.launches() + args.steps     # + one DA update per step
+  del la0
+  secs = sum(tm['step_ms']) / 1000.0
+  secs, grad_evals = replicas.combine_throughput(secs, tm['lf'])   # max time, total work
   value = grad_evals / secs
-  draws_t = torch.stack(draws)
-  min_ess_per_s = None
-  if args.steps >= 20:   # cross-chain ESS (diagnostic.py:220-275) over the timed draws
-    ess = pg.mcmc.effective_sample_size(draws_t, filter_beyond_positive_pairs=True,
-                                        cross_chain_dims=1)
-    min_ess_per_s = float(ess.min().item()) / secs
-  # Split R-hat (diagnostic.py:339,517-543) over the timed draws, max over
-  # dimensions; a diagnostic of the short timed window, not a convergence claim.
-  rhat_max = None
-  if args.steps >= 4:
-    try:
-      rhat_max = float(pg.mcmc.potential_scale_reduction(draws_t, split_chains=True).max().item())
-    except Exception:   # a diagnostic must never fail the benchmark line
-      rhat_max = None
+  ess_s = min_ess_per_s(pg, tm['draws'], sum(tm['step_ms']) / 1000.0)
+  rhat = split_rhat_max(pg, tm['draws'])
+  sm_max = (clk or {}).get('sm_max_mhz') or peaks.get('sm_max_mhz', 2070.0)
+  # Profiled pass: the next K transitions, leaf by leaf with events.
+  q, kr, prof = leg.profiled(q, kr, keys_for(args.steps, args.warmup + args.steps))
+  roofline = leg_roofline(leg, prof, args.workload, w['d'], sm_max,
+                          'a profiled pass of %d further transitions (events around every '
+                          'batched gradient; the timed region replays graphs)' % args.steps)
 
-  # ---- roofline of the dominant kernel (batched gradient) ----
-  flops_per_grad, bytes_per_batch = target.cost(1)
-  alg_flops = flops_per_grad * int(lf_prof.item())
-  peaks, peak_src = read_peaks()
-  eval_s = prof_ms.value / 1000.0
-  achieved_tflops = alg_flops / eval_s / 1e12 if eval_s > 0 else None
-  tensor_peak = peaks['bf16_tflops']
-  kernel_name = ('logreg_partial_kernel' if target.precision == 'fp32' else
-                 'logreg_tc_pair_kernel' if w['d'] > 256 else
-                 'logreg_tc_kernel' if w['d'] > 128 else 'logreg_tct_kernel')
-  roofline = {
-      'bound': 'tensor', 'achieved': achieved_tflops, 'peak': tensor_peak, 'unit': 'TFLOP/s',
-      'frac': achieved_tflops / tensor_peak if achieved_tflops else None,
-      'traffic': read_traffic(args.workload, kernel_name), 'kernel': kernel_name,
-      'peak_source': peak_src + ' (MEASURED_PEAKS.json bf16_tflops burst)',
-      'eval_launches': int(prof_evals.value), 'eval_ms_total': prof_ms.value,
-      'alg_flops_per_grad_eval': flops_per_grad,
-      'measured_over': 'a profiled pass of %d transitions after the timed region (events '
-                       'around every batched gradient; the timed region replays graphs)'
-                       % args.steps,
-  }
-  if target.precision == 'fp32':
-    roofline['note'] = ('FP32 CUDA-core kernel (plain FP32 form); the roof shown is the BF16 '
-                        'tensor-core peak, so frac understates its use of the FP32 pipes')
-
-  # ---- end-to-end through host buffers ----
-  C, D = state.shape
+  # ---- end-to-end through host buffers (public API, pinned memory) ----
+  C, D = q.shape
   h_state = torch.empty((C, D), dtype=torch.float32).pin_memory()
   h_tlp = torch.empty(C, dtype=torch.float64).pin_memory()
   h_grad = torch.empty((C, D), dtype=torch.float32).pin_memory()
   h_out = torch.empty((C, D), dtype=torch.float32).pin_memory()
   h_lar = torch.empty(C, dtype=torch.float64).pin_memory()
-  h_state.copy_(state.cpu())
-  h_tlp.copy_(kr.inner_results.target_log_prob.cpu())
-  h_grad.copy_(kr.inner_results.grads_target_log_prob.cpu())
-  e2e_steps = max(1, args.steps)
+  h_state.copy_(start_q.cpu())
+  h_tlp.copy_(start_kr.inner_results.target_log_prob.cpu())
+  h_grad.copy_(start_kr.inner_results.grads_target_log_prob.cpu())
+  kr = start_kr
+  e2e_keys = keys_for(args.warmup + args.steps)[args.warmup:]
+  if laplace:   # the same transitions again, from the host-resident start
+    q_, kr_, _ = leg.run(start_q.clone(), start_kr, keys_for(args.warmup), timed=False)
+    h_state.copy_(q_.cpu())
+    h_tlp.copy_(kr_.inner_results.target_log_prob.cpu())
+    h_grad.copy_(kr_.inner_results.grads_target_log_prob.cpu())
+    kr = kr_
   lf_e2e = torch.zeros((), dtype=torch.int64, device=dev)
   barrier()
   e0 = torch.cuda.Event(enable_timing=True)
   e1 = torch.cuda.Event(enable_timing=True)
   e0.record()
-  for _ in range(e2e_steps):
+  for key in e2e_keys:
     d_state = h_state.to(dev, non_blocking=True)
     inner = kr.inner_results._replace(
         target_log_prob=h_tlp.to(dev, non_blocking=True),
         grads_target_log_prob=h_grad.to(dev, non_blocking=True))
     kr = kr._replace(inner_results=inner)
-    state, kr = step(d_state, kr, t)
-    t += 1
+    s_, kr = leg.kernel.one_step(d_state, kr, seed=key)
     lf_e2e += kr.inner_results.leapfrogs_taken.sum()
-    h_out.copy_(state, non_blocking=True)
+    h_out.copy_(s_, non_blocking=True)
     h_lar.copy_(kr.inner_results.log_accept_ratio, non_blocking=True)
     h_tlp.copy_(kr.inner_results.target_log_prob, non_blocking=True)
     h_grad.copy_(kr.inner_results.grads_target_log_prob, non_blocking=True)
@@ -604,39 +873,37 @@ def run_engine(args, w):
   h2d = C * D * 4 * 2 + C * 8
   d2h = C * D * 4 * 2 + C * 8 * 2
 
-  # ---- the plain FP32 form on the same GPU, from the same adapted state ----
-  plain = None
-  if w['d'] > 256:
-    plain = {'value': None, 'note': 'the FP32 CUDA-core target supports up to 256 features'}
-  elif target.precision != 'fp32' and args.plain_steps > 0:
-    t32 = pg.LogisticRegression(X, y, precision='fp32')
-    eps = kr.new_step_size.reshape(-1)[0].item()
-    n32 = pg.mcmc.NoUTurnSampler(t32, step_size=eps, max_tree_depth=w['depth'])
-    s32 = state.clone()
-    k32 = n32.bootstrap_results(s32)
-    for i in range(2):
-      s32, k32 = n32.one_step(s32, k32, seed=pg._util.step_key(seed, 10**6 + i))
-    lf32 = torch.zeros((), dtype=torch.int64, device=dev)
+  # ---- the other precision on the same GPU, same start and transitions ----
+  other = None
+  other_prec = 'mixed' if precision == 'fp32' else 'fp32'
+  if args.other_precision and not (other_prec == 'fp32' and w['d'] > 256):
+    X_other = X if other_prec == 'fp32' else X_engine
+    leg2 = Leg(pg, X_other, y, w, other_prec, eps, dev)
+    leg2.prewarm(state0, args.prewarm, (w['seed'], 1))
+    q2, kr2 = leg2.start(start_q)
+    kr2 = kr2._replace(inner_results=kr2.inner_results)
+    q2, kr2, _ = leg2.run(q2, kr2, keys_for(args.warmup), timed=False)
     barrier()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record()
-    for i in range(args.plain_steps):
-      s32, k32 = n32.one_step(s32, k32, seed=pg._util.step_key(seed, 2 * 10**6 + i))
-      lf32 += k32.leapfrogs_taken.sum()
-    e1.record()
-    e1.synchronize()
-    s = e0.elapsed_time(e1) / 1000.0
-    plain = {'value': int(lf32.item()) / s, 'unit': 'grad-evals/s',
-             'ms_per_step': 1000 * s / args.plain_steps, 'steps': args.plain_steps,
-             'note': 'NoUTurnSampler with the FP32 CUDA-core target at the adapted step size, '
-                     'started from the same chain state'}
+    q2, kr2, tm2 = leg2.run(q2, kr2, keys_for(args.steps, args.warmup), l2_flush=l2_flush)
+    secs2 = sum(tm2['step_ms']) / 1000.0
+    q2, kr2, prof2 = leg2.profiled(q2, kr2, keys_for(args.steps, args.warmup + args.steps))
+    ess2 = min_ess_per_s(pg, tm2['draws'], secs2)
+    other = {'precision': other_prec, 'value': tm2['lf'] / secs2, 'unit': 'grad-evals/s',
+             'ms_per_step': 1000 * secs2 / args.steps, 'min_ess_per_s': ess2,
+             'roofline': leg_roofline(leg2, prof2, args.workload, w['d'], sm_max,
+                                      'a profiled pass of %d further transitions'
+                                      % args.steps),
+             'note': 'same start state, step size and transition keys as the main line'}
+    if precision == 'fp32':
+      other['speedup_vs_fp32_grad_evals'] = other['value'] / value
+      other['speedup_vs_fp32_min_ess_per_s'] = (ess2 / ess_s) if ess2 and ess_s else None
+    del leg2
 
   cpu = None
   if rank == 0 and world == 1 and not args.no_cpu_baseline and w['n'] * w['d'] > 5e7:
     budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '20'))
     sub = 64
-    rate, nev, dt = cpu_gradient_rate(X, y, state[:sub].cpu().numpy(), budget)
+    rate, nev, dt = cpu_gradient_rate(X, y, start_q[:sub].cpu().numpy(), budget)
     cpu = {'value': rate, 'unit': 'grad-evals/s', 'cores': os.cpu_count(), 'kind': 'port',
            'sample': '%d batched log-prob+gradient evaluations of %d of the %d chains '
                      '(%.1f s; the NUTS leaf cost, no tree bookkeeping); float32 torch '
@@ -644,61 +911,78 @@ def run_engine(args, w):
   elif rank == 0 and world == 1 and not args.no_cpu_baseline:
     budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '20'))
     sub = 64
-    rate, nsteps, dt = cpu_baseline_run(w, X, y, init, budget, 1000000,
-                                        state=state[:sub].cpu().numpy(),
-                                        step_size=float(kr.new_step_size.reshape(-1)[0].item()))
+    rate, nsteps, dt = cpu_nuts_run(w, X, y, init[:sub], eps, keys_for(10 ** 4), budget)
     cpu = {'value': rate, 'unit': 'grad-evals/s', 'cores': os.cpu_count(), 'kind': 'port',
-           'sample': '%d DA(NUTS) transitions of %d of the %d chains, started from the '
-                     'engine\'s adapted state and step size (%.1f s); oracle NUTS in NumPy '
-                     '(chains in lock-step as in the reference), float32 target on torch CPU '
-                     'ops, all host threads'
-                     % (nsteps, sub, w['chains'], dt)}
+           'sample': '%d NUTS transitions of chains 0-%d of %d (%.1f s), from the same start, '
+                     'step size and transition keys as the timed region (the same draws); '
+                     'oracle NUTS in NumPy (chains in lock-step as in the reference), float32 '
+                     'target on torch CPU ops, all host threads'
+                     % (nsteps, sub - 1, w['chains'], dt)}
 
-  prec = None
+  prec_report = None
   if rank == 0 and w.get('precision_report'):
-    prec = precision_report(target, X_engine, y, w['precision_report'], w['seed'], dev)
+    prec_report = precision_report(leg.target, X_engine, y, w['precision_report'], w['seed'],
+                                   dev)
 
   if rank == 0:
+    wall = sum(tm['wall_s'])
     line = {
         'metric': METRIC, 'value': value, 'unit': 'grad-evals/s', 'n_gpus': world,
-        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': step_ms / args.steps,
+        'steps': args.steps, 'warmup': args.warmup, 'ms_per_step': 1000 * secs / args.steps,
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
-        'dtype': 'f32' if target.precision == 'fp32' else 'bf16+f32',
+        'dtype': 'f32' if precision == 'fp32' else 'bf16+f32',
         'data': 'synthetic (seeded numpy default_rng(%d))' % w['seed'],
-        'config': {'workload': args.workload, 'rows': w['n'], 'features': w['d'],
-                   'chains': w['chains'], 'max_tree_depth': w['depth'],
-                   'target_accept_prob': w['target_accept'],
-                   'num_adaptation_steps': w['num_adaptation_steps'],
-                   'precision': target.precision, 'warm_in_transitions': args.warm_in,
-                   'l2': 'flushed between timed steps (256 MB write outside the step events)',
-                   'parallelism': 'replicas' if world > 1 else 'single'},
-        'min_ess_per_s': min_ess_per_s,
-        'split_rhat_max_timed_draws': rhat_max,
-        # Lane-gradients over the profiled pass: the engine evaluates only the
-        # chains still building (compacted batches), so executed = useful; a
-        # lock-step implementation that masks finished chains evaluates
-        # chains x leaf iterations.
+        'config': nuts_config(args, w, precision, world),
+        'min_ess_per_s': ess_s,
+        'split_rhat_max_timed_draws': rhat,
         'lane_grads_profiled_pass': {
-            'useful': int(lf_prof.item()), 'executed': int(lf_prof.item()),
-            'lockstep_masked': w['chains'] * leaves_prof if leaves_prof else None,
-            'leaf_iterations': leaves_prof, 'transitions': args.steps},
-        'step_size': float(kr.new_step_size.reshape(-1)[0].item()),
+            'useful': prof['lf'], 'executed': prof['lf'],
+            'lockstep_masked': w['chains'] * prof['leaves'] if prof['leaves'] else None,
+            'leaf_iterations': prof['leaves'], 'transitions': args.steps},
+        'step_size': eps,
         'mean_leapfrogs_per_chain_step': grad_evals / (args.steps * w['chains'] * world),
-        'wall_s_timed_region': wall,
+        'host_wall_s_timed_steps': wall,
         'e2e': {'value': e2e_value, 'unit': 'grad-evals/s', 'h2d_bytes_per_step': h2d,
-                'd2h_bytes_per_step': d2h, 'steps': e2e_steps},
+                'd2h_bytes_per_step': d2h, 'steps': len(e2e_keys),
+                'transitions': 'the timed transitions again, state in pinned host memory'},
         'roofline': roofline,
         'cpu_baseline': cpu,
-        'plain_fp32': plain,
-        'speedup_vs_plain_fp32': (value / plain['value']) if plain and plain['value'] else None,
-        'gpu_launches': int(launches.value) + args.steps,
+        'other_precision': other,
+        'gpu_launches': launches,
         'clocks': clk,
     }
-    if prec is not None:
-      line['precision_vs_fp64'] = prec
+    if prec_report is not None:
+      line['precision_vs_fp64'] = prec_report
     print(json.dumps(line), flush=True)
   if dist is not None:
     dist.destroy_process_group()
+
+
+def run_adapt(args, w):
+  """Dual averaging over the whole adaptation window (num_adaptation_steps
+  DA(NUTS) transitions, device loop) from the Laplace start at the initial
+  step size; prints the step size the draws phase uses.  This is how the
+  workloads' step_size_draws constants were obtained."""
+  import torch
+  import probability_gb300 as pg
+  X, y, _ = make_data(w)
+  init = laplace_start(X, y, w['chains'], w['seed'])
+  precision = args.precision or w['precision']
+  target = pg.LogisticRegression(engine_features(X, w), y, precision=precision)
+  nuts = pg.mcmc.NoUTurnSampler(target, step_size=w['step0'], max_tree_depth=w['depth'])
+  kernel = pg.mcmc.DualAveragingStepSizeAdaptation(
+      nuts, num_adaptation_steps=w['num_adaptation_steps'],
+      target_accept_prob=w['target_accept'])
+  t0 = time.perf_counter()
+  run = pg.mcmc.run_chain(kernel, 1, torch.from_numpy(init).cuda(),
+                          num_burnin_steps=w['num_adaptation_steps'] - 1, seed=(w['seed'], 0))
+  torch.cuda.synchronize()
+  lar = run.trace['log_accept_ratio'].exp().clamp(max=1.0).mean().item()
+  print(json.dumps({'adapt': args.workload, 'precision': precision,
+                    'transitions': w['num_adaptation_steps'],
+                    'step_size_draws': float(run.final_step_size.reshape(-1)[0].item()),
+                    'last_mean_accept_prob': lar, 'seconds': time.perf_counter() - t0}),
+        flush=True)
 
 
 def make_batch_members(w):
@@ -1000,8 +1284,13 @@ def main():
   ap.add_argument('--workload', default='nuts_logreg_1e5x100', choices=sorted(WORKLOADS))
   ap.add_argument('--precision', default=None, choices=[None, 'fp32', 'mixed'])
   ap.add_argument('--no-cpu-baseline', action='store_true')
-  ap.add_argument('--plain-steps', type=int, default=10,
-                  help='transitions of the plain FP32 form timed beside the mixed path')
+  ap.add_argument('--other-precision', type=int, default=1,
+                  help='also time the other precision (mixed beside FP32) on the same '
+                       'transitions')
+  ap.add_argument('--prewarm', type=int, default=6,
+                  help='discarded transitions that capture leaf graphs before timing')
+  ap.add_argument('--adapt', action='store_true',
+                  help='run the adaptation window and print the draws-phase step size')
   ap.add_argument('--kernel-only', action='store_true',
                   help='time the batched log-prob+gradient alone (profiling aid)')
   ap.add_argument('--precondition', action='store_true',
@@ -1010,7 +1299,9 @@ def main():
                   help='with --kernel-only: rows of X (default: the workload\'s)')
   args = ap.parse_args()
   w = WORKLOADS[args.workload]
-  if args.impl == 'reference':
+  if args.adapt:
+    run_adapt(args, w)
+  elif args.impl == 'reference':
     run_reference(args, w)
   elif args.kernel_only and not args.workload.startswith('nuts_batch'):
     run_kernel_only(args, w)

@@ -123,6 +123,10 @@ bool batch_schedule(const Target* t, int32_t* chain_tile);
 
 std::unique_ptr<Target> make_transformed(gbm_context* ctx, Target* inner, const int32_t* codes);
 
+// FP32 target for up to 128 features (row-pair layout, bulk-copied tiles);
+// nullptr above that.
+std::unique_ptr<Target> make_logreg_f32(gbm_context* ctx, const float* X, int64_t n, int64_t d,
+                                        const float* y, float prior_scale);
 std::unique_ptr<Target> make_logreg_simt(gbm_context* ctx, const float* X, int64_t n,
                                          int64_t d, const float* y, float prior_scale);
 

@@ -290,6 +290,7 @@ namespace {
 std::unique_ptr<Target> make_logreg_simt(gbm_context* ctx, const float* X, int64_t n, int64_t d,
                                          const float* y, float prior_scale) {
   if (d > 256) return nullptr;
+  if (d <= 128) return make_logreg_f32(ctx, X, n, d, y, prior_scale);
   return std::unique_ptr<Target>(new LogregSimt(ctx, X, n, d, y, prior_scale));
 }
 
