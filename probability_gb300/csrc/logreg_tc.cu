@@ -11,8 +11,11 @@
 // residual X_lo for FP32 data up to 128 features); the FP32 chain states B
 // are split into a BF16 high part and a BF16 residual and both are
 // multiplied (residual correction), so Z -- and therefore the log-density
-// that drives acceptance -- carries ~16 significant bits of the states.  R
-// enters the gradient contraction as BF16.  A gradient that is a
+// that drives acceptance -- carries ~16 significant bits of the states.  In
+// the chain-major kernel (D <= 128) the gradient contraction is corrected
+// the same way: R is split into BF16 hi + lo and G = R_hi^T X_hi +
+// R_lo^T X_hi (+ R_hi^T X_lo for FP32 data); above 128 features R enters
+// the gradient contraction as BF16.  A gradient that is a
 // deterministic function of the state keeps the leapfrog map reversible and
 // volume-preserving, so the sampler stays exact; only its acceptance rate
 // depends on the gradient's accuracy.
@@ -537,13 +540,15 @@ __device__ __forceinline__ float neg_copysign(float w, float h) {
 //   *sarg += arg (so sum |h| = -sarg / (2 log2 e)),
 //   *prod *= u,
 //   R = (y - 1/2) - tanh(h)/2 with tanh(|h|)/2 = 1/u - 1/2 (rcp.approx,
-//     within one ulp), packed as BF16 pairs (round to nearest).
+//     within one ulp), split into BF16 hi = bf16(R) and lo = bf16(R - hi)
+//     (round to nearest), packed as pairs: the gradient contraction's
+//     residual correction, R = hi + lo to ~2^-17.
 // MASK: rows at or past `nvalid` are padding (X = 0) and leave both sums
 // unchanged.
 template <bool MASK>
 __device__ __forceinline__ void tct_rows(const float (&h)[32], const float* __restrict__ ys,
                                          int nvalid, float2* sarg, float2* prod,
-                                         uint32_t (&rp)[16]) {
+                                         uint32_t (&rp)[16], uint32_t (&rl)[16]) {
   const float2 one = f2(1.f, 1.f), mhalf = f2(-0.5f, -0.5f);
   float2 sa = f2(0.f, 0.f), pr = f2(1.f, 1.f);
 #pragma unroll
@@ -563,7 +568,10 @@ __device__ __forceinline__ void tct_rows(const float (&h)[32], const float* __re
       const float2 w = __fadd2_rn(f2(tc::rcp_approx(u.x), tc::rcp_approx(u.y)), mhalf);
       const float2 ym = e == 0 ? f2(yv.x, yv.y) : f2(yv.z, yv.w);
       const float2 r = __fadd2_rn(ym, f2(neg_copysign(w.x, h[j]), neg_copysign(w.y, h[j + 1])));
-      rp[2 * g + e] = pack_bf16x2(r.x, r.y);
+      const __nv_bfloat162 rh = __floats2bfloat162_rn(r.x, r.y);
+      rp[2 * g + e] = *reinterpret_cast<const uint32_t*>(&rh);
+      const float2 rhf = __bfloat1622float2(rh);
+      rl[2 * g + e] = pack_bf16x2(r.x - rhf.x, r.y - rhf.y);
     }
   }
   *sarg = sa;
@@ -737,10 +745,15 @@ logreg_tct_kernel(const __grid_constant__ CUtensorMap xmap,
         const uint32_t tr = tmem + kTZ + b * 128;
 #pragma unroll
         for (int ks = 0; ks < kRows / 16; ++ks) {
-          // Rows 16 ks .. 16 ks + 15: row block ks / 2, half ks % 2.
-          tc::mma_bf16_tmem_a(tmem + kTG, tr + (ks >> 1) * 32 + (ks & 1) * 8,
-                              xs + (uint64_t)((ks * 2048) >> 4), idesc2,
-                              (it > 0 || ks > 0) ? 1u : 0u);
+          // Rows 16 ks .. 16 ks + 15: row block ks / 2, half ks % 2; R_hi at
+          // column offset 0 of the block, R_lo at 16.  G^T += R_hi^T X_hi +
+          // R_lo^T X_hi (+ R_hi^T X_lo for FP32 data).
+          const uint32_t ra = tr + (ks >> 1) * 32 + (ks & 1) * 8;
+          const uint64_t bx = xs + (uint64_t)((ks * 2048) >> 4);
+          tc::mma_bf16_tmem_a(tmem + kTG, ra, bx, idesc2, (it > 0 || ks > 0) ? 1u : 0u);
+          tc::mma_bf16_tmem_a(tmem + kTG, ra + 16, bx, idesc2, 1u);
+          if constexpr (XLO)
+            tc::mma_bf16_tmem_a(tmem + kTG, ra, bx + (32768 >> 4), idesc2, 1u);
         }
         tc::mma_commit(&bars->x_empty[s]);
         if (it + 2 < T) {
@@ -790,10 +803,10 @@ logreg_tct_kernel(const __grid_constant__ CUtensorMap xmap,
       }
       const int nvalid = N - ((rt_begin + it) * kRows + rblk * 32);
       const float* ys = Ys + s * kRows + rblk * 32;
-      uint32_t rp[16];
+      uint32_t rp[16], rl[16];
       float2 sarg, prod;
-      if (nvalid >= 32) tct_rows<false>(h, ys, 32, &sarg, &prod, rp);
-      else tct_rows<true>(h, ys, nvalid, &sarg, &prod, rp);
+      if (nvalid >= 32) tct_rows<false>(h, ys, 32, &sarg, &prod, rp, rl);
+      else tct_rows<true>(h, ys, nvalid, &sarg, &prod, rp, rl);
       {
         const float sabs = (sarg.x + sarg.y) * kArgToAbsH;
         const float v = fmaf(kLn2, tc::lg2_approx(prod.x * prod.y), sabs) - comp;
@@ -801,8 +814,10 @@ logreg_tct_kernel(const __grid_constant__ CUtensorMap xmap,
         comp = (t - acc) - v;
         acc = t;
       }
-      // R^T over the first 16 of this warp's 32 Z^T columns (already loaded).
+      // R^T over this warp's 32 Z^T columns (already loaded): hi in the
+      // first 16, lo in the last 16.
       tc::tmem_st16(tz, rp);
+      tc::tmem_st16(tz + 16, rl);
       tc::tmem_st_wait();
       tc::tc_fence_before();
       __syncwarp();
