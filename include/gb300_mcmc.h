@@ -79,10 +79,14 @@ GBM_API int gbm_step_key(const uint32_t seed[2], uint64_t step, uint32_t out[2])
  * (mcmc/internal/util.py:286-308, math/gradient.py:28) for the
  * inference_gym logistic-regression target
  * (spinoffs/inference_gym/inference_gym/targets/logistic_regression.py:92-103,
- * distributions/bernoulli.py:126-140).  X and y are copied.  Limits:
- * num_features <= 256 for precision GBM_PRECISION_F32 (float32 X), <= 512 for
- * GBM_PRECISION_MIXED (float32 or BF16 X; above 256 features a 2-CTA cluster
- * shares each tile). */
+ * distributions/bernoulli.py:126-140).  X and y are copied.  Kernels by
+ * feature count: GBM_PRECISION_F32 (float32 X) runs fused CUDA-core kernels
+ * up to 256 features; GBM_PRECISION_MIXED (float32 or BF16 X) fused tcgen05
+ * kernels up to 512 (above 256 a 2-CTA cluster shares each tile).  Beyond
+ * those limits the two contractions are cuBLAS GEMMs (FP32 accumulation; the
+ * mixed form keeps the BF16 hi/lo residual correction) around this
+ * library's element-wise kernels, and every evaluation covers all the
+ * chains of the call.  num_rows < 2^31. */
 GBM_API int gbm_target_logistic_regression(gbm_context* ctx, const void* x, int x_dtype,
                                    int64_t num_rows, int64_t num_features, const float* y,
                                    float prior_scale, int precision, gbm_target** out);
@@ -260,6 +264,19 @@ GBM_API int gbm_nuts_set_graphs(gbm_nuts* kernel, int enable);
  * squared deviations (float64, Welford) after `count_before` samples. */
 GBM_API int gbm_moments_update(gbm_context* ctx, const float* state, int64_t elements,
                                int64_t count_before, double* mean, double* m2);
+/* Streaming autocovariance for the effective sample size
+ * (mcmc/diagnostic.py:203-337 with filter_beyond_lag = max_lag) without
+ * storing draws: fold one state of `elements` float32 values, the
+ * (count_before + 1)-th draw, into per-element running sums.  With E =
+ * elements and L = max_lag, the caller's zero-initialised device arrays are
+ * first [E] and head, ring [L][E] (float32), total [E] and lag_sums [L+1][E]
+ * (float64): first holds x_0, head the first L and ring the last L draws
+ * (ring[t mod L]); with y_t = x_t - x_0 in float64, total = sum y_t and
+ * lag_sums[k] = sum_{t >= k} y_t y_{t-k} -- from which the centred
+ * autocovariance at lags 0..L follows exactly. */
+GBM_API int gbm_autocov_update(gbm_context* ctx, const float* state, int64_t elements,
+                               int64_t count_before, int32_t max_lag, float* first,
+                               double* total, float* head, float* ring, double* lag_sums);
 /* Diagonal mass matrix for subsequent gbm_nuts_one_step calls, as
  * tfp.experimental.mcmc.PreconditionedNoUTurnSampler
  * (experimental/mcmc/preconditioned_nuts.py:169) with the momentum
@@ -423,6 +440,40 @@ GBM_API int gbm_dual_averaging_update(gbm_context* ctx, int64_t chains, const do
                               double target_accept_scalar, const double* target_accept_prob,
                               double exploration_shrinkage, double step_count_smoothing,
                               double decay_rate, double* state, float* step_size);
+
+/* The same update with the chains' log accept probabilities already reduced
+ * by the caller: reduced_log_accept_prob is float64 [groups], the value of
+ * DualAveragingStepSizeAdaptation's reduce_fn (reduce_logmeanexp by default;
+ * e.g. reduce_log_harmonic_mean_exp or a maximum, as the reference allows,
+ * dual_averaging_step_size_adaptation.py:141,410-422) applied to
+ * min(log_accept_ratio, 0) (non-finite -> -inf). */
+GBM_API int gbm_dual_averaging_update_reduced(gbm_context* ctx, int64_t groups,
+                                              const double* reduced_log_accept_prob,
+                                              int32_t num_adaptation_steps,
+                                              double target_accept_scalar,
+                                              const double* target_accept_prob,
+                                              double exploration_shrinkage,
+                                              double step_count_smoothing, double decay_rate,
+                                              double* state, float* step_size);
+
+/* ---- MetropolisHastings ----------------------------------------------- */
+
+/* MetropolisHastings.one_step's accept/reject for a proposal an inner kernel
+ * already made (mcmc/metropolis_hastings.py:160-254): log_accept_ratio =
+ * proposed - current target log-prob + log_acceptance_correction (NULL: 0),
+ * non-finite -> -inf (safe_sum, mcmc/internal/util.py:213-235); accept iff
+ * log U < log_accept_ratio with U the transition's Metropolis-Hastings
+ * uniform for `seed` (the draw gbm_hmc_one_step uses, so wrapping the
+ * uncalibrated HMC proposal reproduces gbm_hmc_one_step exactly);
+ * next_state = accepted ? proposed : current ([chains][dim] float32). */
+GBM_API int gbm_metropolis_hastings_step(gbm_context* ctx, int64_t chains, int64_t dim,
+                                         const uint32_t seed[2],
+                                         const double* current_target_log_prob,
+                                         const double* proposed_target_log_prob,
+                                         const double* log_acceptance_correction,
+                                         const float* current_state, const float* proposed_state,
+                                         float* next_state, double* log_accept_ratio,
+                                         uint8_t* is_accepted);
 
 #ifdef __cplusplus
 }

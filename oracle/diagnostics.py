@@ -21,14 +21,18 @@ def auto_covariance(x, axis=0):
   return np.moveaxis(r, -1, axis)
 
 
-def effective_sample_size(states, filter_threshold=0.0,
+def effective_sample_size(states, filter_threshold=0.0, filter_beyond_lag=None,
                           filter_beyond_positive_pairs=False,
                           cross_chain_dims=None):
   """diagnostic.py:203-337.  With cross_chain_dims=None the result has the
-  chain axis (sum it for a total ESS, as nuts_test.py:398-399 does)."""
+  chain axis (sum it for a total ESS, as nuts_test.py:398-399 does).
+  filter_beyond_lag keeps lags 0..filter_beyond_lag of the autocorrelation
+  (the max_lags of auto_correlation, diagnostic.py:254-258)."""
   states = np.asarray(states, np.float64)
   n = states.shape[0]
   acov = auto_covariance(states, 0)
+  if filter_beyond_lag is not None:
+    acov = acov[:int(filter_beyond_lag) + 1]
   if cross_chain_dims is not None:
     ax = cross_chain_dims
     num_chains = states.shape[ax]

@@ -59,11 +59,15 @@ _SIGNATURES = {
     'gbm_nuts_set_profiling': ([P, ctypes.c_int], ctypes.c_int),
     'gbm_nuts_set_graphs': ([P, ctypes.c_int], ctypes.c_int),
     'gbm_moments_update': ([P, P, I64, I64, P, P], ctypes.c_int),
+    'gbm_autocov_update': ([P, P, I64, I64, I32, P, P, P, P, P], ctypes.c_int),
     'gbm_nuts_set_inverse_mass': ([P, P, ctypes.c_int], ctypes.c_int),
     'gbm_nuts_read_profile': ([P, ctypes.POINTER(F64), ctypes.POINTER(I64),
                                ctypes.POINTER(I64)], ctypes.c_int),
     'gbm_dual_averaging_update': (
         [P, I64, P, ctypes.c_int, I32, F64, P, F64, F64, F64, P, P], ctypes.c_int),
+    'gbm_dual_averaging_update_reduced': (
+        [P, I64, P, I32, F64, P, F64, F64, F64, P, P], ctypes.c_int),
+    'gbm_metropolis_hastings_step': ([P, I64, I64, U32P] + [P] * 8, ctypes.c_int),
     'gbm_step_key': ([U32P, ctypes.c_uint64, U32P], ctypes.c_int),
     'gbm_nuts_sample_chain': ([P, I64, P, P, P, P, ctypes.c_int, U32P, I64, I64, I64, I64, I32,
                                F64, F64, F64, F64] + [P] * 8, ctypes.c_int),

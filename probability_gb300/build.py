@@ -28,6 +28,11 @@ def nvcc():
   return cand
 
 
+def cuda_libdir(cc):
+  """lib64 of the CUDA toolkit that owns `cc` (runtime path of cuBLAS)."""
+  return os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(cc))), 'lib64')
+
+
 def sources():
   return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith('.cu'))
 
@@ -60,7 +65,8 @@ def build(verbose=False, ptxas_info=False):
     objs = list(ex.map(compile_one, srcs))
   out = os.path.join(LIBDIR, LIBNAME)
   tmp = out + '.tmp'
-  cmd = [cc, '-shared', '-o', tmp] + objs + ARCH + ['-lcudart']
+  cmd = [cc, '-shared', '-o', tmp] + objs + ARCH + ['-lcudart', '-lcublas',
+                                                     '-Xlinker', '-rpath=' + cuda_libdir(cc)]
   r = subprocess.run(cmd, capture_output=True, text=True)
   if r.returncode != 0:
     raise RuntimeError('link failed:\n%s\n%s' % (' '.join(cmd), r.stderr))

@@ -166,12 +166,18 @@ int gbm_target_logistic_regression(gbm_context* ctx, const void* x, int x_dtype,
       }
       t->impl = gbm::make_logreg_simt(ctx, static_cast<const float*>(x), num_rows, num_features,
                                       y, prior_scale);
+      if (!t->impl)   // above 256 features: library GEMMs + fused element-wise kernels
+        t->impl = gbm::make_logreg_large(ctx, x, x_dtype, num_rows, num_features, y,
+                                         prior_scale, false);
       if (!t->impl) {
         delete t;
-        return invalid("gbm_target_logistic_regression: FP32 path supports num_features <= 256");
+        return invalid("gbm_target_logistic_regression: shape out of range");
       }
     } else {
       t->impl = gbm::make_logreg_tc(ctx, x, x_dtype, num_rows, num_features, y, prior_scale);
+      if (!t->impl)   // above 512 features
+        t->impl = gbm::make_logreg_large(ctx, x, x_dtype, num_rows, num_features, y,
+                                         prior_scale, true);
       if (!t->impl) {
         delete t;
         set_error("gbm_target_logistic_regression: mixed-precision path unavailable for this shape");
@@ -574,6 +580,21 @@ int gbm_moments_update(gbm_context* ctx, const float* state, int64_t elements,
   });
 }
 
+int gbm_autocov_update(gbm_context* ctx, const float* state, int64_t elements,
+                       int64_t count_before, int32_t max_lag, float* first, double* total,
+                       float* head, float* ring, double* lag_sums) {
+  if (!ctx || !state || !first || !total || !head || !ring || !lag_sums)
+    return invalid("gbm_autocov_update: NULL argument");
+  if (elements <= 0 || count_before < 0 || max_lag < 1 || max_lag > 4096)
+    return invalid("gbm_autocov_update: bad sizes (1 <= max_lag <= 4096)");
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    gbm::autocov_update(ctx->stream, state, (size_t)elements, count_before, max_lag, first,
+                        total, head, ring, lag_sums);
+    return GBM_OK;
+  });
+}
+
 int gbm_nuts_set_graphs(gbm_nuts* k, int enable) {
   if (!k) return invalid("gbm_nuts_set_graphs: NULL argument");
   k->use_graphs = enable != 0;
@@ -625,6 +646,47 @@ int gbm_dual_averaging_update(gbm_context* ctx, int64_t chains, const double* la
                       decay_rate, num_adaptation_steps};
     gbm::dual_averaging_update(ctx->stream, lar, chains, per_chain, prm, target_accept_prob,
                                state, step_size);
+    return GBM_OK;
+  });
+}
+
+int gbm_dual_averaging_update_reduced(gbm_context* ctx, int64_t groups,
+                                      const double* reduced_log_accept_prob,
+                                      int32_t num_adaptation_steps, double target_accept_scalar,
+                                      const double* target_accept_prob,
+                                      double exploration_shrinkage, double step_count_smoothing,
+                                      double decay_rate, double* state, float* step_size) {
+  if (!ctx || !reduced_log_accept_prob || !state || !step_size)
+    return invalid("gbm_dual_averaging_update_reduced: NULL argument");
+  if (groups <= 0) return invalid("gbm_dual_averaging_update_reduced: groups must be > 0");
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    gbm::DaParams prm{target_accept_scalar, exploration_shrinkage, step_count_smoothing,
+                      decay_rate, num_adaptation_steps};
+    gbm::dual_averaging_update_reduced(ctx->stream, reduced_log_accept_prob, groups, prm,
+                                       target_accept_prob, state, step_size);
+    return GBM_OK;
+  });
+}
+
+int gbm_metropolis_hastings_step(gbm_context* ctx, int64_t chains, int64_t dim,
+                                 const uint32_t seed[2], const double* current_target_log_prob,
+                                 const double* proposed_target_log_prob,
+                                 const double* log_acceptance_correction,
+                                 const float* current_state, const float* proposed_state,
+                                 float* next_state, double* log_accept_ratio,
+                                 uint8_t* is_accepted) {
+  if (!ctx || !seed || !current_target_log_prob || !proposed_target_log_prob ||
+      !current_state || !proposed_state || !next_state || !log_accept_ratio || !is_accepted)
+    return invalid("gbm_metropolis_hastings_step: NULL argument");
+  if (chains <= 0 || chains > (1 << 24) || dim <= 0)
+    return invalid("gbm_metropolis_hastings_step: bad chains or dim");
+  return guarded([&] {
+    DeviceGuard g(ctx->device);
+    gbm::metropolis_hastings_step(ctx->stream, chains, dim, make_uint2(seed[0], seed[1]),
+                                  current_target_log_prob, proposed_target_log_prob,
+                                  log_acceptance_correction, current_state, proposed_state,
+                                  next_state, log_accept_ratio, is_accepted);
     return GBM_OK;
   });
 }

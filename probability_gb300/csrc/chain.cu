@@ -64,6 +64,43 @@ __global__ void moments_update_kernel(const float* __restrict__ x, size_t n, dou
   m2[i] += delta * (v - mnew);
 }
 
+// Running lagged products for a streaming autocovariance (the effective
+// sample size of mcmc/diagnostic.py:203-337 truncated at lag L =
+// filter_beyond_lag, without storing draws).  Per element e, draws are shifted
+// by the first draw, y_t = x_t - x_0 in float64 (exact for float32 draws;
+// autocovariance is shift-invariant and the shift keeps the float64 sums from
+// cancelling).  Kept: x_0, total = sum y_t, head[j] = x_j for j < L,
+// ring[t mod L] = x_t for the last L draws (float32 draws as given), and
+// lag[k] = sum_{t >= k} y_t y_{t-k} for k = 0..L.  Arrays are
+// [slot][elements] so each update is coalesced.
+__global__ void autocov_update_kernel(const float* __restrict__ x, size_t E, int64_t n, int L,
+                                      float* __restrict__ x0, double* __restrict__ total,
+                                      float* __restrict__ head, float* __restrict__ ring,
+                                      double* __restrict__ lag) {
+  const size_t e = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= E) return;
+  const float xe = x[e];
+  if (n == 0) x0[e] = xe;
+  const double base = (double)(n == 0 ? xe : x0[e]);
+  const double yd = (double)xe - base;
+  total[e] += yd;
+  lag[e] += yd * yd;
+  const int kmax = n < (int64_t)L ? (int)n : L;
+  for (int k = 1; k <= kmax; ++k) {
+    const double yk = (double)ring[(size_t)((n - k) % L) * E + e] - base;
+    lag[(size_t)k * E + e] += yd * yk;
+  }
+  if (n < (int64_t)L) head[(size_t)n * E + e] = xe;
+  ring[(size_t)(n % L) * E + e] = xe;
+}
+
+void autocov_update(cudaStream_t s, const float* x, size_t E, int64_t count_before, int L,
+                    float* x0, double* total, float* head, float* ring, double* lag) {
+  autocov_update_kernel<<<(unsigned)((E + 255) / 256), 256, 0, s>>>(
+      x, E, count_before, L, x0, total, head, ring, lag);
+  GBM_CUDA(cudaGetLastError());
+}
+
 // The key of the transition at the device-side step counter, then advance it
 // (so a captured transition can be replayed for every step).
 __global__ void advance_step_key_kernel(uint2 seed, uint32_t* step, uint2* key) {

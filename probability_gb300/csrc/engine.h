@@ -123,6 +123,11 @@ bool batch_schedule(const Target* t, int32_t* chain_tile);
 
 std::unique_ptr<Target> make_transformed(gbm_context* ctx, Target* inner, const int32_t* codes);
 
+// Any feature count, from library GEMMs (cuBLAS) and fused element-wise
+// kernels: the FP32 target above 256 features, the mixed one above 512.
+std::unique_ptr<Target> make_logreg_large(gbm_context* ctx, const void* X, int x_dtype, int64_t n,
+                                          int64_t d, const float* y, float prior_scale,
+                                          bool mixed);
 // FP32 target for up to 128 features (row-pair layout, bulk-copied tiles);
 // nullptr above that.
 std::unique_ptr<Target> make_logreg_f32(gbm_context* ctx, const float* X, int64_t n, int64_t d,

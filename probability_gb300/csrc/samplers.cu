@@ -460,13 +460,52 @@ __global__ void hmc_finish_kernel(HmcDev w, const float* __restrict__ q0,
   }
 }
 
+// MetropolisHastings.one_step's correction for a proposal another kernel made
+// (metropolis_hastings.py:160-254): log_accept_ratio = safe_sum(proposed -
+// current + correction) (non-finite -> -inf), accept iff log U < ratio with
+// U the transition's MH uniform (the draw hmc_finish_kernel uses, so
+// MetropolisHastings(UncalibratedHamiltonianMonteCarlo) reproduces
+// HamiltonianMonteCarlo bit for bit), next = accepted ? proposed : current.
+__global__ void mh_accept_kernel(int C, int D, uint2 key, const double* __restrict__ cur_tlp,
+                                 const double* __restrict__ prop_tlp,
+                                 const double* __restrict__ corr,
+                                 const float* __restrict__ cur_q, const float* __restrict__ prop_q,
+                                 float* __restrict__ next_q, double* __restrict__ lar_out,
+                                 uint8_t* __restrict__ acc_out) {
+  const int c = warp_id(), lane = threadIdx.x & 31;
+  if (c >= C) return;
+  double lar = prop_tlp[c] - cur_tlp[c] + (corr ? corr[c] : 0.0);
+  if (!isfinite(lar)) lar = -INFINITY;
+  const float U = draw_uniform(key, draw_site(kDrawMhUniform, 0, 0), (uint32_t)c);
+  const bool acc = log((double)U) < lar;
+  const size_t o = (size_t)c * D;
+  for (int d = lane; d < D; d += 32) next_q[o + d] = acc ? prop_q[o + d] : cur_q[o + d];
+  if (lane == 0) {
+    lar_out[c] = lar;
+    acc_out[c] = acc ? 1 : 0;
+  }
+}
+
+void metropolis_hastings_step(cudaStream_t s, int64_t C, int64_t D, uint2 key,
+                              const double* cur_tlp, const double* prop_tlp, const double* corr,
+                              const float* cur_q, const float* prop_q, float* next_q,
+                              double* lar, uint8_t* acc) {
+  mh_accept_kernel<<<warp_blocks(C), 32 * kWarpsPerBlock, 0, s>>>(
+      (int)C, (int)D, key, cur_tlp, prop_tlp, corr, cur_q, prop_q, next_q, lar, acc);
+  GBM_CUDA(cudaGetLastError());
+}
+
 // --------------------------------------------------------------------------
 // Dual averaging (dual_averaging_step_size_adaptation.py:353-475)
 // --------------------------------------------------------------------------
 // state: [groups][4] doubles = error_sum, log_averaging_step, log_shrinkage_target, step.
+// `reduced` (optional, float64 [groups]): the caller's reduction of the log
+// accept probabilities (a custom reduce_fn, :141,410-422); `lar` is then
+// unused.
 __global__ void dual_averaging_kernel(const double* __restrict__ lar, int C, int per_chain,
                                       DaParams prm, const double* __restrict__ target_accept,
-                                      double* __restrict__ state, float* __restrict__ eps) {
+                                      double* __restrict__ state, float* __restrict__ eps,
+                                      const double* __restrict__ reduced, int groups) {
   __shared__ double red[32];
   __shared__ double bcast;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
@@ -497,6 +536,10 @@ __global__ void dual_averaging_kernel(const double* __restrict__ lar, int C, int
     st[3] = step;
     eps[g] = ns;
   };
+  if (reduced) {
+    for (int g = tid; g < groups; g += blockDim.x) update(g, reduced[g]);
+    return;
+  }
   if (per_chain) {
     for (int c = tid; c < C; c += blockDim.x) update(c, lap(c));
     return;
@@ -819,7 +862,16 @@ void hmc_step_launches(gbm_hmc* k, int64_t chains, const float* q, const double*
 void dual_averaging_update(cudaStream_t s, const double* lar, int64_t C, int per_chain,
                            const DaParams& prm, const double* target_accept, double* state,
                            float* eps) {
-  dual_averaging_kernel<<<1, 1024, 0, s>>>(lar, (int)C, per_chain, prm, target_accept, state, eps);
+  dual_averaging_kernel<<<1, 1024, 0, s>>>(lar, (int)C, per_chain, prm, target_accept, state, eps,
+                                           nullptr, 0);
+  GBM_CUDA(cudaGetLastError());
+}
+
+void dual_averaging_update_reduced(cudaStream_t s, const double* reduced, int64_t groups,
+                                   const DaParams& prm, const double* target_accept,
+                                   double* state, float* eps) {
+  dual_averaging_kernel<<<1, 1024, 0, s>>>(nullptr, 0, 0, prm, target_accept, state, eps,
+                                           reduced, (int)groups);
   GBM_CUDA(cudaGetLastError());
 }
 

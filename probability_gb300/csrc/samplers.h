@@ -102,6 +102,8 @@ struct ChainTrace {
 
 // Fold one state [n elements] into running moments after `count_before`
 // earlier samples (Welford).
+void autocov_update(cudaStream_t s, const float* x, size_t E, int64_t count_before, int L,
+                    float* x0, double* total, float* head, float* ring, double* lag);
 void moments_update(cudaStream_t s, const float* x, size_t n, int64_t count_before, double* mean,
                     double* m2);
 
@@ -130,6 +132,13 @@ void hmc_step_launches(gbm_hmc* k, int64_t chains, const float* q, const double*
 void hmc_one_step(gbm_hmc* k, int64_t chains, const float* q, const double* l, const float* g,
                   const float* eps, int per_chain, int num_leapfrog_steps, uint2 key,
                   const HmcOutputs& out);
+void metropolis_hastings_step(cudaStream_t s, int64_t C, int64_t D, uint2 key,
+                              const double* cur_tlp, const double* prop_tlp, const double* corr,
+                              const float* cur_q, const float* prop_q, float* next_q,
+                              double* lar, uint8_t* acc);
+void dual_averaging_update_reduced(cudaStream_t s, const double* reduced, int64_t groups,
+                                   const DaParams& prm, const double* target_accept,
+                                   double* state, float* eps);
 void dual_averaging_update(cudaStream_t s, const double* lar, int64_t C, int per_chain,
                            const DaParams& prm, const double* target_accept, double* state,
                            float* eps);

@@ -65,9 +65,12 @@ size_t estimate_bytes(const gbm_job_spec& s, int num_sms) {
   if (s.family == GBM_FAMILY_LOGISTIC_REGRESSION) {
     const double N = (double)s.rows;
     const double Dp = std::ceil(D / 64.0) * 64.0;
-    b += (s.precision == GBM_PRECISION_MIXED) ? N * Dp * 4.0 : N * (std::ceil(D / 4.0) * 4.0) * 4.0;
-    b += N * 4.0;
+    const bool mixed = s.precision == GBM_PRECISION_MIXED;
+    b += mixed ? N * Dp * 4.0 : N * (std::ceil(D / 16.0) * 16.0) * 4.0;
+    b += N * 8.0;
     b += (2.0 * num_sms * 128.0 + C) * (8.0 + 4.0 * D);
+    if (D > (mixed ? 512.0 : 256.0))   // library-GEMM target: Z, R (hi + lo), G, cuBLAS
+      b += N * C * (mixed ? 8.0 : 12.0) + C * Dp * 12.0 + (32u << 20);
   } else if (s.family == GBM_FAMILY_MVN) {
     b += 4.0 * D * D + 4.0 * D + C * (8.0 * std::ceil(D / 64.0) + 4.0 * D);
   } else {
@@ -116,6 +119,9 @@ void run_job(gbm_context* ctx, Job* job) {
                     ? make_logreg_tc(ctx, s.x, s.x_dtype, s.rows, s.features, s.y, s.prior_scale)
                     : make_logreg_simt(ctx, static_cast<const float*>(s.x), s.rows, s.features,
                                        s.y, s.prior_scale);
+      if (!t->impl)   // beyond the fused kernels' feature limits
+        t->impl = make_logreg_large(ctx, s.x, s.x_dtype, s.rows, s.features, s.y,
+                                    s.prior_scale, s.precision == GBM_PRECISION_MIXED);
       break;
     case GBM_FAMILY_MVN:
       t->impl = make_mvn(ctx, s.loc, s.scale_tril_inv, s.dim, s.log_normalizer);

@@ -23,16 +23,30 @@ def _auto_covariance(x):
   return r / denom.reshape((-1,) + (1,) * (x.dim() - 1))
 
 
-def effective_sample_size(states, filter_threshold=0., filter_beyond_positive_pairs=False,
-                          cross_chain_dims=None):
+def effective_sample_size(states, filter_threshold=0., filter_beyond_lag=None,
+                          filter_beyond_positive_pairs=False, cross_chain_dims=None):
+  """diagnostic.py:203-337; filter_beyond_lag truncates the autocorrelation
+  at that lag (auto_correlation's max_lags, :254-258)."""
   states = torch.as_tensor(states)
   n = states.shape[0]
   acov = _auto_covariance(states)
+  if filter_beyond_lag is not None:
+    acov = acov[:int(filter_beyond_lag) + 1]
+  means = states.to(torch.float64).mean(0) if cross_chain_dims is not None else None
+  return ess_from_auto_covariance(acov, n, means, filter_threshold,
+                                  filter_beyond_positive_pairs, cross_chain_dims)
+
+
+def ess_from_auto_covariance(acov, n, chain_means=None, filter_threshold=0.,
+                             filter_beyond_positive_pairs=False, cross_chain_dims=None):
+  """The ESS formula of diagnostic.py:242-337 from centred autocovariances
+  acov [lags, ...] of n-draw chains (divided by n - lag); with
+  cross_chain_dims (an axis of the draws, so axis cross_chain_dims - 1 of
+  acov[k]) the chain means give the between-chain variance."""
   if cross_chain_dims is not None:
     ax = int(cross_chain_dims)
-    num_chains = states.shape[ax]
-    means = states.to(torch.float64).mean(0)
-    between = means.var(dim=ax - 1, unbiased=True)
+    num_chains = acov.shape[ax]
+    between = chain_means.var(dim=ax - 1, unbiased=True)
     within = acov[0].mean(dim=ax - 1)
     approx = within + between
     rho = 1.0 - (within - acov.mean(dim=ax)) / approx

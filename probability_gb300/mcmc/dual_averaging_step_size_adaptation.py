@@ -20,13 +20,30 @@ DualAveragingStepSizeAdaptationResults = kernel_base.results_type(
      'num_adaptation_steps', 'new_step_size'])
 
 
-def reduce_logmeanexp(x, axis=None, keepdims=False):
-  """Marker for the default reduction (math/generic.py:221); the engine
-  performs it on the device inside the dual-averaging kernel."""
-  x = torch.as_tensor(x)
-  dims = tuple(range(x.dim())) if axis is None else axis
-  n = x.numel() if axis is None else int(np.prod([x.shape[a] for a in np.atleast_1d(axis)]))
-  return torch.logsumexp(x, dim=dims, keepdim=keepdims) - np.log(n)
+def reduce_logmeanexp(input_tensor, axis=None, keepdims=False, experimental_named_axis=None):
+  """log(mean(exp(x))) over `axis` (math/generic.py:221-275).  The default
+  reduction; for the engine's kernels the dual-averaging kernel performs it
+  on the device itself."""
+  if experimental_named_axis:
+    raise NotImplementedError('the engine runs on one GPU; no named-axis reduction')
+  x = torch.as_tensor(input_tensor)
+  dims = tuple(range(x.dim())) if axis is None else tuple(np.atleast_1d(axis).tolist())
+  if not dims:
+    return x
+  n = int(np.prod([x.shape[a] for a in dims]))
+  m = torch.amax(x, dim=dims, keepdim=True)
+  m = torch.where(torch.isfinite(m), m, torch.zeros_like(m))
+  out = torch.log(torch.sum(torch.exp(x - m), dim=dims, keepdim=True)) + m - np.log(n)
+  return out if keepdims else out.reshape([s for i, s in enumerate(x.shape) if i not in dims])
+
+
+def reduce_log_harmonic_mean_exp(input_tensor, axis=None, keepdims=False,
+                                 experimental_named_axis=None):
+  """log(1 / mean(1 / exp(x))) = -reduce_logmeanexp(-x) (math/generic.py:
+  387-428): the reduction the reference recommends for dual averaging when
+  some chains may be stuck (dual_averaging_step_size_adaptation.py:135-143)."""
+  return -reduce_logmeanexp(-torch.as_tensor(input_tensor), axis=axis, keepdims=keepdims,
+                            experimental_named_axis=experimental_named_axis)
 
 
 def _enable_store_parameters_in_results(kernel):
@@ -58,8 +75,6 @@ class DualAveragingStepSizeAdaptation(kernel_base.TransitionKernel):
         raise ValueError('`target_accept_prob` must be > 0.')
       if np.any(tap >= 1):
         raise ValueError('`target_accept_prob` must be < 1.')
-    if reduce_fn is not reduce_logmeanexp:
-      raise NotImplementedError('only the default reduce_logmeanexp reduction runs on the device')
     if experimental_reduce_chain_axis_names:
       raise NotImplementedError('the engine runs on one GPU; no cross-device chain reduction')
     self._parameters = dict(
@@ -116,10 +131,29 @@ class DualAveragingStepSizeAdaptation(kernel_base.TransitionKernel):
       tap_scalar = float(tap)
     ctx = _native.Context.current()
     P = _native.ptr
-    _native.check(_native.lib().gbm_dual_averaging_update(
-        ctx.handle, lap.numel(), P(lap), per_chain, int(pkr.num_adaptation_steps), tap_scalar,
-        P(tap_t), float(pkr.exploration_shrinkage), float(pkr.step_count_smoothing),
-        float(pkr.decay_rate), P(state), P(eps)), 'gbm_dual_averaging_update')
+    reduce_fn = self._parameters['reduce_fn']
+    if reduce_fn is reduce_logmeanexp or per_chain:
+      # The chain reduction (reduce_logmeanexp over the chain axis, or none
+      # for per-chain step sizes, :410-422) runs inside the kernel.
+      _native.check(_native.lib().gbm_dual_averaging_update(
+          ctx.handle, lap.numel(), P(lap), per_chain, int(pkr.num_adaptation_steps),
+          tap_scalar, P(tap_t), float(pkr.exploration_shrinkage),
+          float(pkr.step_count_smoothing), float(pkr.decay_rate), P(state), P(eps)),
+          'gbm_dual_averaging_update')
+    else:
+      # A custom reduce_fn (:141, 410-422) over the chain axis of the log
+      # accept probabilities min(lar, 0), non-finite -> -inf
+      # (simple_step_size_adaptation.py:42-48), on the device.
+      lp = torch.where(torch.isfinite(lap), lap, torch.full_like(lap, -np.inf)).clamp(max=0.0)
+      try:
+        red = reduce_fn(lp, axis=0, keepdims=False, experimental_named_axis=None)
+      except TypeError:
+        red = reduce_fn(lp, axis=0, keepdims=False)
+      red = _util.as_tensor(red, torch.float64, lap.device).reshape(-1).contiguous()
+      _native.check(_native.lib().gbm_dual_averaging_update_reduced(
+          ctx.handle, 1, P(red), int(pkr.num_adaptation_steps), tap_scalar, P(tap_t),
+          float(pkr.exploration_shrinkage), float(pkr.step_count_smoothing),
+          float(pkr.decay_rate), P(state), P(eps)), 'gbm_dual_averaging_update_reduced')
     shape = tuple(torch.as_tensor(step_size).shape) if not isinstance(step_size, torch.Tensor) \
         else tuple(step_size.shape)
     new_step = eps.reshape(shape)
@@ -129,7 +163,11 @@ class DualAveragingStepSizeAdaptation(kernel_base.TransitionKernel):
         log_averaging_step=sq(state[:, 1]), new_step_size=new_step)
 
   def bootstrap_results(self, init_state):
-    inner_results = self.inner_kernel.bootstrap_results(init_state)
+    return self._bootstrap_from_inner_results(init_state,
+                                              self.inner_kernel.bootstrap_results(init_state))
+
+  def _bootstrap_from_inner_results(self, init_state, inner_results):
+    """:546-609: fresh adaptation state around existing inner results."""
     step_size = self.step_size_getter_fn(inner_results)
     dev = _util.device()
     s = _util.as_tensor(step_size, torch.float32, dev)

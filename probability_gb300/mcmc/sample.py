@@ -30,6 +30,8 @@ def _stack(items):
     return torch.stack(items)
   if isinstance(first, tuple) and hasattr(first, '_fields'):
     return type(first)(*[_stack([it[i] for it in items]) for i in range(len(first))])
+  if isinstance(first, dict):
+    return {k: _stack([it[k] for it in items]) for k in first}
   if isinstance(first, (list, tuple)):
     if len(first) == 0:
       return first
@@ -49,8 +51,12 @@ def _unwrap(kernel):
       DualAveragingStepSizeAdaptation)
   from probability_gb300.mcmc.hmc import HamiltonianMonteCarlo
   from probability_gb300.mcmc.nuts import NoUTurnSampler
+  from probability_gb300.mcmc.dual_averaging_step_size_adaptation import reduce_logmeanexp
   da = None
   if isinstance(kernel, DualAveragingStepSizeAdaptation):
+    if kernel.parameters['reduce_fn'] is not reduce_logmeanexp:
+      # The device loop's adaptation reduces with reduce_logmeanexp.
+      return None, None
     da, kernel = kernel, kernel.inner_kernel
   if isinstance(kernel, (NoUTurnSampler, HamiltonianMonteCarlo)):
     return kernel, da

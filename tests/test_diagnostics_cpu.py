@@ -37,6 +37,17 @@ def test_ess_matches_oracle(rho, kw):
   np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-9)
 
 
+@pytest.mark.parametrize('lag', [1, 10, 64])
+@pytest.mark.parametrize('kw', [{}, {'filter_beyond_positive_pairs': True},
+                                {'cross_chain_dims': 1}])
+def test_ess_filter_beyond_lag_matches_oracle(lag, kw):
+  x = _ar1(257, 6, 3, 0.7, seed=lag)
+  got = diagnostic.effective_sample_size(torch.from_numpy(x), filter_beyond_lag=lag,
+                                         **kw).numpy()
+  want = diagnostics.effective_sample_size(x, filter_beyond_lag=lag, **kw)
+  np.testing.assert_allclose(got, want, rtol=1e-9, atol=1e-9)
+
+
 @pytest.mark.parametrize('split', [False, True])
 @pytest.mark.parametrize('n', [200, 201])
 def test_rhat_matches_oracle(split, n):
