@@ -61,11 +61,11 @@ WORKLOADS['nuts_batch_256'] = dict(mvn=128, hier=128, d_range=(8, 2048), j_range
 # with N ~ log-U[1e3, 2e5] rows, D ~ log-U[10, 1000] features (BF16 X, N(0,
 # 1/D), intercept column), 16-256 chains, 500-5000 draws after 300
 # adaptation steps, admitted under a 150 GB device-memory budget.  The timed
-# sample is the first `requests` jobs of the stream; draws and adaptation
-# steps are multiplied by `length_scale`, and D is capped at the mixed
-# path's 512 features (both stated in the output).
-WORKLOADS['serve_logreg_stream'] = dict(rate=200.0, requests=64, length_scale=0.1, seed=4,
-                                        n_range=(1e3, 2e5), d_range=(10, 1000), d_cap=512,
+# sample is the first `requests` jobs of the stream, at their stated lengths
+# and feature counts (above 512 features the mixed target's contractions
+# are library GEMMs).
+WORKLOADS['serve_logreg_stream'] = dict(rate=200.0, requests=64, length_scale=1.0, seed=4,
+                                        n_range=(1e3, 2e5), d_range=(10, 1000),
                                         chains=(16, 256), draws=(500, 5000), adapt=300,
                                         depth=10, budget_gb=150, workers=16)
 METRIC = 'grad-evals/s (NUTS leapfrogs_taken summed over chains; min-ESS/s reported beside)'
@@ -1181,12 +1181,47 @@ def run_batch(args, w):
   print(json.dumps(line), flush=True)
 
 
+def serve_stream(pg, srv, jobs_spec, inputs, w, host):
+  """Replay the stream through the job server.  host=False: each job's X, y
+  and initial state are already on the device; host=True (end to end): they
+  are uploaded from pinned host memory at submission and each job's draws
+  are copied back to the host when it finishes, inside the timed window."""
+  import torch
+  from probability_gb300.serving import DONE
+  handles = []
+  t0 = time.perf_counter()
+  for js, (X, y, q0) in zip(jobs_spec, inputs):
+    delay = js['t'] - (time.perf_counter() - t0)
+    if delay > 0:
+      time.sleep(delay)
+    if host:
+      # The server's worker streams read these buffers: the upload completes
+      # on the host's stream before the job is submitted.
+      X, y, q0 = X.cuda(), y.cuda(), q0.cuda()
+      torch.cuda.current_stream().synchronize()
+    handles.append(srv.submit_logistic_regression(
+        X, y, q0, js['draws'], precision='mixed', num_burnin_steps=js['adapt'],
+        step_size=0.1, max_tree_depth=w['depth'], num_adaptation_steps=js['adapt'],
+        target_accept_prob=0.8, seed=(w['seed'], js['seed']),
+        trace=('state', 'leapfrogs_taken')))
+  infos, d2h = [], 0
+  for h in handles:
+    infos.append(h.wait(timeout=7200.0))
+    if host:
+      st = h.states.cpu()
+      d2h += st.numel() * 4
+  wall = time.perf_counter() - t0
+  assert all(i['status'] == DONE for i in infos)
+  return handles, infos, wall, d2h
+
+
 def run_serving(args, w):
   """Replay the head of a Poisson request stream through the job server and
-  report latency percentiles, aggregate min-ESS/s and device throughput."""
+  report latency percentiles, aggregate min-ESS/s and device throughput; then
+  the same stream end to end from host memory."""
   import torch
   import probability_gb300 as pg
-  from probability_gb300.serving import Server, DONE
+  from probability_gb300.serving import Server
   world, rank, local = dist_setup(args)
   if rank != 0:
     return
@@ -1194,20 +1229,19 @@ def run_serving(args, w):
   torch.cuda.set_device(dev)
   rng = np.random.default_rng(w['seed'])
   R = int(os.environ.get('GBM_SERVE_REQUESTS', w['requests']))
-  scale = w['length_scale']
+  scale = float(os.environ.get('GBM_SERVE_LENGTH_SCALE', w['length_scale']))
   jobs_spec = []
   t_arr = 0.0
   for i in range(R):
     t_arr += rng.exponential(1.0 / w['rate'])
     n = int(np.exp(rng.uniform(np.log(w['n_range'][0]), np.log(w['n_range'][1]))))
-    d_draw = int(np.exp(rng.uniform(np.log(w['d_range'][0]), np.log(w['d_range'][1]))))
+    d = int(np.exp(rng.uniform(np.log(w['d_range'][0]), np.log(w['d_range'][1]))))
     c = int(rng.integers(w['chains'][0], w['chains'][1] + 1))
     draws = int(rng.integers(w['draws'][0], w['draws'][1] + 1))
-    jobs_spec.append(dict(t=t_arr, n=n, d=min(d_draw, w['d_cap']), d_drawn=d_draw, c=c,
-                          draws=max(1, int(round(draws * scale))),
+    jobs_spec.append(dict(t=t_arr, n=n, d=d, c=c, draws=max(1, int(round(draws * scale))),
                           adapt=max(1, int(round(w['adapt'] * scale))), seed=i))
-  # Data on the device before the clock starts (the server receives device
-  # pointers; generating X is not part of serving).
+  # Inputs: seeded on the device (the device-resident pass does not time
+  # their creation), with pinned host copies for the end-to-end pass.
   g = torch.Generator(device=dev)
   g.manual_seed(w['seed'])
   inputs = []
@@ -1223,51 +1257,91 @@ def run_serving(args, w):
                device=local)
   clocks = ClockSampler(local)
   clocks.start()
-  handles = []
-  t0 = time.perf_counter()
-  srv_t0 = srv.now()
-  for js, (X, y, q0) in zip(jobs_spec, inputs):
-    delay = js['t'] - (time.perf_counter() - t0)
-    if delay > 0:
-      time.sleep(delay)
-    handles.append(srv.submit_logistic_regression(
-        X, y, q0, js['draws'], precision='mixed', num_burnin_steps=js['adapt'],
-        step_size=0.1, max_tree_depth=w['depth'], num_adaptation_steps=js['adapt'],
-        target_accept_prob=0.8, seed=(w['seed'], js['seed']),
-        trace=('state', 'leapfrogs_taken')))
-  infos = [h.wait(timeout=3600.0) for h in handles]
-  wall = time.perf_counter() - t0
+  handles, infos, wall, _ = serve_stream(pg, srv, jobs_spec, inputs, w, host=False)
   clk = clocks.stop()
-  assert all(i['status'] == DONE for i in infos)
   lat = np.array([i['end_s'] - i['submit_s'] for i in infos])
   queue = np.array([i['start_s'] - i['submit_s'] for i in infos])
   busy = max(i['end_s'] for i in infos) - min(i['submit_s'] for i in infos)
-  ess_sum, lf_sum, minstep = 0.0, 0, []
-  for h in handles:
+  ess_sum, lf_sum, flops = 0.0, 0, 0.0
+  for js, h in zip(jobs_spec, handles):
     st = h.states                       # [draws, C, D]
-    lf_sum += int(h.leapfrogs_taken.sum().item())
+    lf = int(h.leapfrogs_taken.sum().item())
+    lf_sum += lf
+    flops += 4.0 * js['n'] * js['d'] * lf
     if st.shape[0] >= 4:
       ess = pg.mcmc.effective_sample_size(st, filter_beyond_positive_pairs=True,
                                           cross_chain_dims=1)
       ess_sum += float(ess.min().item())
+  value = ess_sum / busy
+  del handles
+  e2e = None
+  if args.serve_e2e:
+    host_inputs = [(X.cpu().pin_memory(), y.cpu().pin_memory(), q0.cpu().pin_memory())
+                   for X, y, q0 in inputs]
+    h2, i2, wall2, d2h = serve_stream(pg, srv, jobs_spec, host_inputs, w, host=True)
+    busy2 = max(i['end_s'] for i in i2) - min(i['submit_s'] for i in i2)
+    ess2 = 0.0
+    for h in h2:
+      st = h.states
+      if st.shape[0] >= 4:
+        ess2 += float(pg.mcmc.effective_sample_size(
+            st, filter_beyond_positive_pairs=True, cross_chain_dims=1).min().item())
+    h2d = sum(X.numel() * 2 + y.numel() * 4 + q0.numel() * 4 for X, y, q0 in host_inputs)
+    lat2 = np.array([i['end_s'] - i['submit_s'] for i in i2])
+    e2e = {'value': ess2 / busy2, 'unit': 'ESS/s', 'h2d_bytes_per_step': h2d / R,
+           'd2h_bytes_per_step': d2h / R,
+           'latency_s': {'p50': float(np.percentile(lat2, 50)),
+                         'p99': float(np.percentile(lat2, 99))},
+           'note': 'the same stream with every job\'s X, y and initial state uploaded from '
+                   'pinned host memory at submission and its draws copied back when it '
+                   'finishes (a step is one request)'}
   srv.close()
+  peaks, peak_src = read_peaks()
+  achieved = flops / busy / 1e12
+  roofline = {'bound': 'tensor', 'achieved': achieved, 'peak': peaks['bf16_tflops'],
+              'unit': 'TFLOP/s', 'frac': achieved / peaks['bf16_tflops'], 'traffic': None,
+              'kernel': 'all gradient kernels of the stream (aggregate over the makespan)',
+              'peak_source': peak_src + ' (MEASURED_PEAKS.json bf16_tflops burst)',
+              'note': 'algorithmic 4 N D flops per useful gradient evaluation summed over jobs, '
+                      'divided by the makespan: a whole-stream utilisation (jobs are small and '
+                      'latency-bound; sampler kernels and idle time are in the denominator)'}
+  cpu = None
+  if not args.no_cpu_baseline:
+    # The oracle's batched log-prob + gradient (float32, all host threads) on
+    # the first jobs' data and chains: the CPU cost of one NUTS leaf of those
+    # jobs, turned into ESS/s with the GPU run's ESS per gradient evaluation.
+    budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '20'))
+    evals, secs = 0, 0.0
+    for js, (X, y, q0) in list(zip(jobs_spec, inputs))[:4]:
+      r, _, dt = cpu_gradient_rate(X.float().cpu().numpy(), y.cpu().numpy(),
+                                   q0.cpu().numpy(), budget / 4)
+      evals += r * dt
+      secs += dt
+    rate = evals / secs
+    per_grad_ess = ess_sum / max(lf_sum, 1)
+    cpu = {'value': rate * per_grad_ess, 'unit': 'ESS/s', 'cores': os.cpu_count(),
+           'kind': 'port', 'grad_evals_per_s': rate,
+           'sample': 'batched log-prob+gradient evaluations of the first 4 jobs (%.1f s), '
+                     'float32 torch CPU ops, all host threads; ESS/s = that rate x the '
+                     'stream\'s ESS per gradient evaluation on the GPU' % secs}
   line = {
       'metric': 'aggregate min-ESS/s over a served request stream (p50/p99 latency beside)',
-      'value': ess_sum / busy, 'unit': 'ESS/s', 'n_gpus': 1, 'steps': R, 'warmup': 0,
+      'value': value, 'unit': 'ESS/s', 'n_gpus': 1, 'steps': R, 'warmup': 0,
       'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'bf16+f32',
       'data': 'synthetic (seeded torch generator on the device)',
       'config': {'workload': args.workload, 'arrival_rate_per_s': w['rate'], 'requests': R,
-                 'length_scale': scale, 'd_cap': w['d_cap'],
-                 'jobs_with_d_capped': int(sum(js['d_drawn'] > w['d_cap'] for js in jobs_spec)),
+                 'length_scale': scale, 'max_features': max(js['d'] for js in jobs_spec),
+                 'jobs_above_512_features': int(sum(js['d'] > 512 for js in jobs_spec)),
                  'workers': w['workers'], 'memory_budget_gb': w['budget_gb'],
                  'max_tree_depth': w['depth'],
-                 'note': 'the first %d requests of the Poisson stream; draws and adaptation '
-                         'steps x %.2f of the stated 500-5000 / 300' % (R, scale)},
+                 'note': 'the first %d requests of the Poisson stream at the stated lengths '
+                         '(500-5000 draws after 300 adaptation steps) x %.2f' % (R, scale)},
       'latency_s': {'p50': float(np.percentile(lat, 50)), 'p99': float(np.percentile(lat, 99)),
                     'mean': float(lat.mean()), 'max': float(lat.max())},
       'queue_s': {'p50': float(np.percentile(queue, 50)), 'p99': float(np.percentile(queue, 99))},
       'makespan_s': busy, 'wall_s': wall, 'jobs_per_s': R / busy,
       'grad_evals_per_s': lf_sum / busy,
+      'e2e': e2e, 'roofline': roofline, 'cpu_baseline': cpu,
       'clocks': clk,
   }
   print(json.dumps(line), flush=True)
@@ -1289,6 +1363,8 @@ def main():
                        'transitions')
   ap.add_argument('--prewarm', type=int, default=6,
                   help='discarded transitions that capture leaf graphs before timing')
+  ap.add_argument('--serve-e2e', type=int, default=1,
+                  help='serving: replay the stream again end to end from host memory')
   ap.add_argument('--adapt', action='store_true',
                   help='run the adaptation window and print the draws-phase step size')
   ap.add_argument('--kernel-only', action='store_true',

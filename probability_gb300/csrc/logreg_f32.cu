@@ -159,14 +159,18 @@ logreg_f32_kernel(const float* __restrict__ X2, const float* __restrict__ ym, in
       for (int c = 0; c < 8; ++c) z[i][c] = 0.f;
     const float* xa = xs + (2 * ty) * Dp * 2;        // row pair 2 ty (rows 4 ty, 4 ty + 1)
     const float* xb = xa + Dp * 2;                   // row pair 2 ty + 1
+    const float* bp = Bt + 4 * tx;
+    // Register double buffering: the next feature pair's six loads are in
+    // flight while this pair's 64 FMAs issue (the last iteration re-reads
+    // its own pair instead of reading past the tile).
+    float4 u = lds4(xa), v = lds4(xb);   // x(r0,d) x(r1,d) x(r0,d+1) x(r1,d+1); rows r2, r3
+    float4 b0 = lds4(bp), b1 = lds4(bp + 64), b2 = lds4(bp + kF32CT), b3 = lds4(bp + kF32CT + 64);
 #pragma unroll 2
     for (int d = 0; d < dk; d += 2) {
-      const float4 u = lds4(xa + 2 * d);   // x(r0,d) x(r1,d) x(r0,d+1) x(r1,d+1)
-      const float4 v = lds4(xb + 2 * d);   // rows r2, r3
-      const float4 b0 = lds4(Bt + d * kF32CT + 4 * tx);
-      const float4 b1 = lds4(Bt + d * kF32CT + 64 + 4 * tx);
-      const float4 b2 = lds4(Bt + (d + 1) * kF32CT + 4 * tx);
-      const float4 b3 = lds4(Bt + (d + 1) * kF32CT + 64 + 4 * tx);
+      const int dn = d + 2 < dk ? d + 2 : d;
+      const float4 un = lds4(xa + 2 * dn), vn = lds4(xb + 2 * dn);
+      const float4 b0n = lds4(bp + dn * kF32CT), b1n = lds4(bp + dn * kF32CT + 64);
+      const float4 b2n = lds4(bp + (dn + 1) * kF32CT), b3n = lds4(bp + (dn + 1) * kF32CT + 64);
       const float xr0[4] = {u.x, u.y, v.x, v.y};
       const float xr1[4] = {u.z, u.w, v.z, v.w};
       const float bb0[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
@@ -175,6 +179,7 @@ logreg_f32_kernel(const float* __restrict__ X2, const float* __restrict__ ym, in
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int c = 0; c < 8; ++c) z[i][c] = fmaf(xr1[i], bb1[c], fmaf(xr0[i], bb0[c], z[i][c]));
+      u = un; v = vn; b0 = b0n; b1 = b1n; b2 = b2n; b3 = b3n;
     }
     // ---- epilogue: log-likelihood sums and R ----
     const float4 yv = lds4(Ys + st * kF32RT + 4 * ty);
@@ -214,21 +219,35 @@ logreg_f32_kernel(const float* __restrict__ X2, const float* __restrict__ ym, in
       break;
     }
     // ---- phase 2: G += R^T X_tile ----
+    // Register double buffering of the residual rows and the row pair of X,
+    // as in phase 1.
+    const float* rp = Rs + 4 * cg;
+    const float* xq = xs + 2 * fg;
+    float4 ra0 = lds4(rp), ra1 = lds4(rp + 64), rb0 = lds4(rp + kF32CT),
+           rb1 = lds4(rp + kF32CT + 64);
+    float2 xv[KD];
+#pragma unroll
+    for (int j = 0; j < KD; ++j) xv[j] = *reinterpret_cast<const float2*>(xq + 32 * j);
 #pragma unroll 2
     for (int p = 0; p < kF32RT / 2; ++p) {
-      const float4 ra0 = lds4(Rs + (2 * p) * kF32CT + 4 * cg);
-      const float4 ra1 = lds4(Rs + (2 * p) * kF32CT + 64 + 4 * cg);
-      const float4 rb0 = lds4(Rs + (2 * p + 1) * kF32CT + 4 * cg);
-      const float4 rb1 = lds4(Rs + (2 * p + 1) * kF32CT + 64 + 4 * cg);
+      const int pn = p + 1 < kF32RT / 2 ? p + 1 : p;
+      const float* rn = rp + (2 * pn) * kF32CT;
+      const float4 ra0n = lds4(rn), ra1n = lds4(rn + 64), rb0n = lds4(rn + kF32CT),
+                   rb1n = lds4(rn + kF32CT + 64);
+      float2 xvn[KD];
+#pragma unroll
+      for (int j = 0; j < KD; ++j)
+        xvn[j] = *reinterpret_cast<const float2*>(xq + pn * Dp * 2 + 32 * j);
       const float r0[8] = {ra0.x, ra0.y, ra0.z, ra0.w, ra1.x, ra1.y, ra1.z, ra1.w};
       const float r1[8] = {rb0.x, rb0.y, rb0.z, rb0.w, rb1.x, rb1.y, rb1.z, rb1.w};
-      const float* xp = xs + p * Dp * 2 + 2 * fg;
 #pragma unroll
-      for (int j = 0; j < KD; ++j) {
-        const float2 xv = *reinterpret_cast<const float2*>(xp + 32 * j);
+      for (int j = 0; j < KD; ++j)
 #pragma unroll
-        for (int c = 0; c < 8; ++c) g[c][j] = fmaf(r1[c], xv.y, fmaf(r0[c], xv.x, g[c][j]));
-      }
+        for (int c = 0; c < 8; ++c)
+          g[c][j] = fmaf(r1[c], xv[j].y, fmaf(r0[c], xv[j].x, g[c][j]));
+      ra0 = ra0n; ra1 = ra1n; rb0 = rb0n; rb1 = rb1n;
+#pragma unroll
+      for (int j = 0; j < KD; ++j) xv[j] = xvn[j];
     }
     __syncthreads();   // stage st and R are free
     if (tid == 0 && it + 2 < T) issue(it + 2);

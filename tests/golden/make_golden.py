@@ -1,8 +1,9 @@
 """Regenerate the golden fixtures in this directory from the reference.
 
-Run from the repository root with the reference checkout available:
+Run from the repository root, naming the root of a reference checkout
+(the directory that holds ``tensorflow_probability/``):
 
-    python tests/golden/make_golden.py /root/reference
+    python tests/golden/make_golden.py <reference-root>
 
 TensorFlow is not installed here, so the reference's ``nuts.py`` cannot be
 imported as a module.  Its two instruction-table builders
@@ -76,4 +77,6 @@ def main(ref_root):
 
 
 if __name__ == '__main__':
-  main(sys.argv[1] if len(sys.argv) > 1 else '/root/reference')
+  if len(sys.argv) != 2:
+    sys.exit('usage: python tests/golden/make_golden.py <reference-root>')
+  main(sys.argv[1])
