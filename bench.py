@@ -876,7 +876,9 @@ def run_engine(args, w):
   # ---- the other precision on the same GPU, same start and transitions ----
   other = None
   other_prec = 'mixed' if precision == 'fp32' else 'fp32'
-  if args.other_precision and not (other_prec == 'fp32' and w['d'] > 256):
+  # (The FP32 form of the 1e6 x 512 workload would need the library-GEMM
+  # target's N x chains buffers, tens of GB: only the stated arithmetic runs.)
+  if args.other_precision and w['n'] * w['d'] <= 5e7:
     X_other = X if other_prec == 'fp32' else X_engine
     leg2 = Leg(pg, X_other, y, w, other_prec, eps, dev)
     leg2.prewarm(state0, args.prewarm, (w['seed'], 1))
@@ -1134,6 +1136,42 @@ def run_batch(args, w):
                                       ctypes.byref(la))
   secs = step_ms / 1000.0
   grad_evals = int(lf_total.item())
+  # ---- end to end: the same sampler call with the ragged state, its
+  # log-densities and gradients copied in from pinned host memory and back
+  # every step (a bounded number of further transitions) ----
+  e2e = None
+  e2e_steps = min(args.steps, 5)
+  if e2e_steps > 0:
+    h_q = q.cpu().pin_memory()
+    h_l = kr.target_log_prob.cpu().pin_memory()
+    h_g = kr.grads_target_log_prob.cpu().pin_memory()
+    lf_e = torch.zeros((), dtype=torch.int64, device=dev)
+    torch.cuda.synchronize()
+    f0 = torch.cuda.Event(enable_timing=True)
+    f1 = torch.cuda.Event(enable_timing=True)
+    f0.record(batch.stream)
+    for _ in range(e2e_steps):
+      with torch.cuda.stream(batch.stream):
+        dq = h_q.to(dev, non_blocking=True)
+        kr = kr._replace(target_log_prob=h_l.to(dev, non_blocking=True),
+                         grads_target_log_prob=h_g.to(dev, non_blocking=True))
+      q2, kr = k.one_step(dq, kr, seed=pg._util.step_key((w['seed'], 0), t))
+      t += 1
+      with torch.cuda.stream(batch.stream):
+        lf_e += kr.leapfrogs_taken.sum()
+        h_q.copy_(q2, non_blocking=True)
+        h_l.copy_(kr.target_log_prob, non_blocking=True)
+        h_g.copy_(kr.grads_target_log_prob, non_blocking=True)
+      batch.stream.synchronize()
+    f1.record(batch.stream)
+    f1.synchronize()
+    e2e_s = f0.elapsed_time(f1) / 1000.0
+    E, C = batch.elements, batch.chains
+    e2e = {'value': int(lf_e.item()) / e2e_s, 'unit': 'grad-evals/s',
+           'h2d_bytes_per_step': E * 8 + C * 8, 'd2h_bytes_per_step': E * 8 + C * 8,
+           'steps': e2e_steps,
+           'transitions': 'BatchedNoUTurnSampler.one_step with the ragged state, log-densities '
+                          'and gradients copied in from pinned host memory and back every step'}
   ess_sum = None
   if args.steps >= 20:
     D = torch.stack(draws)                  # [steps, elements]
@@ -1176,7 +1214,7 @@ def run_batch(args, w):
                    'kernel': 'batch_phase_kernel (whole sampler step timed)',
                    'peak_source': 'nominal FP32 FMA rate at the maximum SM clock'},
       'setup_s': setup_s, 'gpu_launches': int(la.value), 'clocks': clk,
-      'cpu_baseline': cpu,
+      'cpu_baseline': cpu, 'e2e': e2e,
   }
   print(json.dumps(line), flush=True)
 
