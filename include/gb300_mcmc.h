@@ -242,8 +242,36 @@ GBM_API int gbm_nuts_one_step(gbm_nuts* kernel, int64_t chains, const float* sta
                       int32_t* leapfrogs_taken, uint8_t* is_accepted, uint8_t* reach_max_depth,
                       uint8_t* has_divergence, double* energy, int32_t* tree_depth);
 
+/* Free-running NoUTurnSampler transitions.  No single reference call: each
+ * chain runs `transitions_per_chain` transitions of NoUTurnSampler.one_step
+ * (mcmc/nuts.py:321-445) with keys gbm_step_key(seed, first_step + t) -- the
+ * transitions sample_chain (mcmc/sample.py:81-383) would run at a fixed step
+ * size -- but not in lock-step: a chain starts its next transition as soon as
+ * its own trajectory ends, so one chain building a depth-10 tree does not
+ * hold every other chain for 1023 leaves.  Per chain the results equal the
+ * lock-step sampler's with the same keys.  One leaf iteration advances every
+ * running chain by one leapfrog step; the run stops when every chain has
+ * finished or after max_leaf_iterations (chains are then left mid-way and
+ * transitions_done says how many each completed).  Inputs as
+ * gbm_nuts_one_step (step_size [1] or [chains]); unrolled_leapfrog_steps
+ * must be 1.  Device outputs, each may be NULL: transitions_done int32
+ * [chains]; trace [transitions_per_chain][...] of the completed transitions:
+ * states (float32, [state elements] each), target log-probs, log-accept
+ * ratios (float64 [chains]), leapfrogs taken (int32), accepted and
+ * divergence flags (uint8).  leaf_iterations (host, may be NULL): the
+ * iterations run. */
+GBM_API int gbm_nuts_run_free(gbm_nuts* kernel, int64_t chains, const float* state,
+                              const double* target_log_prob, const float* grads_target_log_prob,
+                              const float* step_size, int step_size_per_chain,
+                              const uint32_t seed[2], int64_t first_step,
+                              int32_t transitions_per_chain, int64_t max_leaf_iterations,
+                              int32_t* transitions_done, float* trace_state,
+                              double* trace_target_log_prob, double* trace_log_accept_ratio,
+                              int32_t* trace_leapfrogs_taken, uint8_t* trace_is_accepted,
+                              uint8_t* trace_has_divergence, int64_t* leaf_iterations);
+
 /* Number of leaf iterations (batched gradient evaluations) the last
- * gbm_nuts_one_step launched. */
+ * gbm_nuts_one_step (or gbm_nuts_run_free) launched. */
 GBM_API int gbm_nuts_last_leaf_iterations(const gbm_nuts* kernel, int64_t* out);
 
 /* Profiling of NUTS transitions.  When enabled, CUDA events on the context

@@ -56,6 +56,8 @@ _SIGNATURES = {
     'gbm_nuts_destroy': ([P], ctypes.c_int),
     'gbm_nuts_one_step': ([P, I64, P, P, P, P, ctypes.c_int, U32P] + [P] * 10, ctypes.c_int),
     'gbm_nuts_last_leaf_iterations': ([P, ctypes.POINTER(I64)], ctypes.c_int),
+    'gbm_nuts_run_free': ([P, I64, P, P, P, P, ctypes.c_int, U32P, I64, I32, I64] + [P] * 7 +
+                          [ctypes.POINTER(I64)], ctypes.c_int),
     'gbm_nuts_set_profiling': ([P, ctypes.c_int], ctypes.c_int),
     'gbm_nuts_set_graphs': ([P, ctypes.c_int], ctypes.c_int),
     'gbm_moments_update': ([P, P, I64, I64, P, P], ctypes.c_int),

@@ -239,6 +239,27 @@ class BatchedNoUTurnSampler:
         leapfrogs_taken=lf, is_accepted=acc.bool(), reach_max_depth=rmd.bool(),
         has_divergence=div.bool(), energy=energy, seed=_util.seed_tensor(seed))
 
+  def run_free(self, current_state, kernel_results, transitions_per_chain, seed,
+                 first_step=0, max_leaf_iterations=1 << 40):
+    """Free-running transitions of every member's chains (no lock-step
+    across chains or members: a chain starts its next transition as soon as
+    its own trajectory ends), per chain equal to one_step with keys
+    step_key(seed, first_step + t).  Returns FreeRun(all_states [K, elements]
+    (ragged, as the state), trace of [K, chains] tensors, transitions_done,
+    leaf_iterations)."""
+    from probability_gb300.mcmc.nuts import run_free
+    b = self.batch
+    q = _util.as_tensor(current_state, torch.float32).reshape(-1).contiguous()
+    eps = self._eps(kernel_results.step_size).contiguous()
+    b._enter()
+    try:
+      run = run_free(self._handle, q, kernel_results, eps, 1, _util.sanitize_seed(seed),
+                     first_step, transitions_per_chain, max_leaf_iterations, (q.numel(),))
+    finally:
+      b._leave()
+    self.last_leaf_iterations = run.leaf_iterations
+    return run
+
 
 class MemberMassMatrixAdaptation:
   """DiagonalMassMatrixAdaptation (experimental/mcmc/

@@ -485,6 +485,49 @@ int gbm_nuts_one_step(gbm_nuts* k, int64_t chains, const float* state,
   });
 }
 
+int gbm_nuts_run_free(gbm_nuts* k, int64_t chains, const float* state,
+                      const double* target_log_prob, const float* grads,
+                      const float* step_size, int step_size_per_chain, const uint32_t seed[2],
+                      int64_t first_step, int32_t transitions_per_chain,
+                      int64_t max_leaf_iterations, int32_t* transitions_done,
+                      float* trace_state, double* trace_target_log_prob,
+                      double* trace_log_accept_ratio, int32_t* trace_leapfrogs_taken,
+                      uint8_t* trace_is_accepted, uint8_t* trace_has_divergence,
+                      int64_t* leaf_iterations) {
+  if (!k || !state || !target_log_prob || !grads || !step_size || !seed)
+    return invalid("gbm_nuts_run_free: NULL argument");
+  if (chains <= 0 || chains > k->max_chains)
+    return invalid("gbm_nuts_run_free: chains must be in [1, max_chains]");
+  if (k->dev.ragged && chains != k->target->impl->ragged_chains())
+    return invalid("gbm_nuts_run_free: a batch target's sampler runs exactly its chains");
+  if (transitions_per_chain < 1 || max_leaf_iterations < 1)
+    return invalid("gbm_nuts_run_free: need transitions_per_chain >= 1 and "
+                   "max_leaf_iterations >= 1");
+  if (k->unrolled_leapfrog_steps != 1)
+    return invalid("gbm_nuts_run_free: needs unrolled_leapfrog_steps == 1");
+  if (first_step < 0 || first_step + transitions_per_chain > ((int64_t)1 << 32))
+    return invalid("gbm_nuts_run_free: step indices must fit 32 bits");
+  return guarded([&] {
+    DeviceGuard g(k->target->ctx->device);
+    gbm::check_device_error(k->target->ctx);
+    gbm::FreeDev f{};
+    f.tr_state = trace_state;
+    f.tr_logp = trace_target_log_prob;
+    f.tr_lar = trace_log_accept_ratio;
+    f.tr_lf = trace_leapfrogs_taken;
+    f.tr_acc = trace_is_accepted;
+    f.tr_div = trace_has_divergence;
+    f.tr_estride = k->dev.ragged ? (size_t)k->target->impl->ragged_elements()
+                                 : (size_t)chains * (size_t)k->target->impl->dim;
+    const int64_t it = gbm::nuts_run_free(
+        k, chains, state, target_log_prob, grads, step_size, step_size_per_chain,
+        make_uint2(seed[0], seed[1]), (uint32_t)first_step, transitions_per_chain,
+        max_leaf_iterations, f, transitions_done);
+    if (leaf_iterations) *leaf_iterations = it;
+    return GBM_OK;
+  });
+}
+
 int gbm_nuts_last_leaf_iterations(const gbm_nuts* k, int64_t* out) {
   if (!k || !out) return invalid("gbm_nuts_last_leaf_iterations: NULL argument");
   *out = k->last_leaf_iterations;

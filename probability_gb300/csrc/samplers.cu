@@ -120,11 +120,15 @@ static void build_active(const NutsDev& d, uint8_t bit, cudaStream_t s) {
 // --------------------------------------------------------------------------
 // NUTS kernels
 // --------------------------------------------------------------------------
-__global__ void nuts_init_kernel(NutsDev w, const float* __restrict__ q,
-                                 const double* __restrict__ l, const float* __restrict__ g,
-                                 const float* __restrict__ eps_in, int eps_per_chain, uint2 key) {
-  const int c = warp_id(), lane = threadIdx.x & 31;
-  if (c >= w.C) return;
+// The kernels below are thin launches of per-chain bodies (one warp, or one
+// thread, per chain) shared by the lock-step transition (all chains at the
+// same depth and leaf) and the free-running loop (every chain at its own).
+
+// Momentum draw and trajectory start of chain c from (q, l, g)
+// (nuts.py:512-539); q may alias cand_q (the free-running loop starts each
+// transition from the previous one's result).
+__device__ void nuts_chain_init(const NutsDev& w, int c, int lane, const float* q, const double* l,
+                                const float* g, float eps_c, uint2 key) {
   const int D = vdim(w, c);
   const size_t o = voff(w, c);
   const uint32_t site = draw_site(kDrawMomentum, 0, 0);
@@ -150,14 +154,21 @@ __global__ void nuts_init_kernel(NutsDev w, const float* __restrict__ q,
     w.cand_l[c] = lc; w.cand_e[c] = e0; w.cand_w[c] = 0.0;
     w.e0[c] = e0; w.eds[c] = 0.0; w.lf[c] = 0; w.tree_depth[c] = 0;
     w.flags[c] = kCont | kNotDiv;
-    w.eps[c] = eps_of(eps_in, eps_per_chain, c);
+    w.eps[c] = eps_c;
   }
 }
 
-__global__ void nuts_depth_begin_kernel(NutsDev w, uint2 key, int depth) {
-  if (blockIdx.x == 0 && threadIdx.x == 0) *w.any_cont = 0;
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+__global__ void nuts_init_kernel(NutsDev w, const float* __restrict__ q,
+                                 const double* __restrict__ l, const float* __restrict__ g,
+                                 const float* __restrict__ eps_in, int eps_per_chain, uint2 key) {
+  const int c = warp_id(), lane = threadIdx.x & 31;
   if (c >= w.C) return;
+  nuts_chain_init(w, c, lane, q, l, g, eps_of(eps_in, eps_per_chain, c), key);
+}
+
+// Start of a tree depth for chain c (one thread): direction draw and the
+// subtree's initial state (nuts.py:551-558, 727-731).
+__device__ void nuts_chain_depth_begin(const NutsDev& w, int c, uint2 key, int depth) {
   uint8_t f = w.flags[c];
   if (!(f & kCont)) {
     w.flags[c] = f & (uint8_t)~(kSubCont | kForward);
@@ -173,20 +184,28 @@ __global__ void nuts_depth_begin_kernel(NutsDev w, uint2 key, int depth) {
   w.tree_depth[c] += 1;
 }
 
-__global__ void nuts_zero_cumsum_kernel(NutsDev w) {
-  const int c = warp_id(), lane = threadIdx.x & 31;
-  if (c >= w.C || !(w.flags[c] & kSubCont)) return;
+__global__ void nuts_depth_begin_kernel(NutsDev w, uint2 key, int depth) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) *w.any_cont = 0;
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= w.C) return;
+  nuts_chain_depth_begin(w, c, key, depth);
+}
+
+__device__ void nuts_chain_zero_cumsum(const NutsDev& w, int c, int lane) {
   const size_t o = voff(w, c);
   const int D = vdim(w, c);
   for (int d = lane; d < D; d += 32) w.cumsum[o + d] = 0.f;
 }
 
-// Half kick + drift for the active chains; writes the dense batch qw.
+__global__ void nuts_zero_cumsum_kernel(NutsDev w) {
+  const int c = warp_id(), lane = threadIdx.x & 31;
+  if (c >= w.C || !(w.flags[c] & kSubCont)) return;
+  nuts_chain_zero_cumsum(w, c, lane);
+}
+
+// Half kick + drift of chain c (batch position j); writes the dense batch qw.
 // leapfrog_integrator.py:280-286 (half kick) and :330-334 (drift).
-__global__ void nuts_leaf_pre_kernel(NutsDev w) {
-  const int j = warp_id(), lane = threadIdx.x & 31;
-  if (j >= *w.act_count) return;
-  const int c = w.act_idx[j];
+__device__ void nuts_chain_leaf_pre(const NutsDev& w, int c, int j, int lane) {
   const int side = (w.flags[c] & kForward) ? 1 : 0;
   const float e = (side ? 1.f : -1.f) * w.eps[c];
   const float he = 0.5f * e;
@@ -202,6 +221,12 @@ __global__ void nuts_leaf_pre_kernel(NutsDev w) {
     Q[o + d] = qn;
     w.qw[oj + d] = qn;
   }
+}
+
+__global__ void nuts_leaf_pre_kernel(NutsDev w) {
+  const int j = warp_id(), lane = threadIdx.x & 31;
+  if (j >= *w.act_count) return;
+  nuts_chain_leaf_pre(w, w.act_idx[j], j, lane);
 }
 
 // Between the unrolled leapfrog steps of one leaf: full kick then drift.
@@ -225,13 +250,9 @@ __global__ void nuts_leaf_mid_kernel(NutsDev w) {
 // Final kick, slot bookkeeping, U-turn checks, energy, multinomial leaf
 // sampling: _loop_build_sub_tree (nuts.py:793-946) and
 // has_not_u_turn_at_all_index (nuts.py:949-984).
-__global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp, int depth,
-                                      int leaf, int wslot, int r0, int r1,
-                                      double max_energy_diff) {
-  const int j = warp_id(), lane = threadIdx.x & 31;
-  if (j >= *w.act_count) return;
-  const uint2 key = *keyp;
-  const int c = w.act_idx[j];
+__device__ void nuts_chain_leaf_post(const NutsDev& w, int c, int j, int lane, uint2 key,
+                                     int depth, int leaf, int wslot, int r0, int r1,
+                                     double max_energy_diff) {
   const int D = vdim(w, c);
   const uint8_t f = w.flags[c];
   const int side = (f & kForward) ? 1 : 0;
@@ -307,13 +328,19 @@ __global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp,
   }
 }
 
+__global__ void nuts_leaf_post_kernel(NutsDev w, const uint2* __restrict__ keyp, int depth,
+                                      int leaf, int wslot, int r0, int r1,
+                                      double max_energy_diff) {
+  const int j = warp_id(), lane = threadIdx.x & 31;
+  if (j >= *w.act_count) return;
+  nuts_chain_leaf_post(w, w.act_idx[j], j, lane, *keyp, depth, leaf, wslot, r0, r1,
+                       max_energy_diff);
+}
+
 // Tree-level biased progressive sampling and trajectory U-turn check
-// (nuts.py:597-711).
-__global__ void nuts_depth_end_kernel(NutsDev w, uint2 key, int depth) {
-  const int c = warp_id(), lane = threadIdx.x & 31;
-  if (c >= w.C) return;
+// (nuts.py:597-711) of a chain whose trajectory continues.
+__device__ void nuts_chain_depth_end(const NutsDev& w, int c, int lane, uint2 key, int depth) {
   const uint8_t f = w.flags[c];
-  if (!(f & kCont)) return;
   const int D = vdim(w, c);
   const size_t o = voff(w, c);
   const bool sub_cont = f & kSubCont;
@@ -353,26 +380,145 @@ __global__ void nuts_depth_end_kernel(NutsDev w, uint2 key, int depth) {
   }
 }
 
+__global__ void nuts_depth_end_kernel(NutsDev w, uint2 key, int depth) {
+  const int c = warp_id(), lane = threadIdx.x & 31;
+  if (c >= w.C) return;
+  if (!(w.flags[c] & kCont)) return;
+  nuts_chain_depth_end(w, c, lane, key, depth);
+}
+
+// NUTSKernelResults of chain c (nuts.py:424-441); NULL outputs are skipped.
+__device__ void nuts_chain_finalize(const NutsDev& w, int c, int lane, const NutsOutputs& out,
+                                    int unrolled) {
+  const size_t o = voff(w, c);
+  const int D = vdim(w, c);
+  for (int d = lane; d < D; d += 32) {
+    if (out.state) out.state[o + d] = w.cand_q[o + d];
+    if (out.grads) out.grads[o + d] = w.cand_g[o + d];
+  }
+  if (lane == 0) {
+    const uint8_t f = w.flags[c];
+    if (out.target_log_prob) out.target_log_prob[c] = w.cand_l[c];
+    if (out.log_accept_ratio)
+      out.log_accept_ratio[c] = log(w.eds[c] / (double)w.lf[c]);   // nuts.py:429-432
+    if (out.leapfrogs_taken) out.leapfrogs_taken[c] = w.lf[c] * unrolled;
+    if (out.is_accepted) out.is_accepted[c] = (f & kAccepted) ? 1 : 0;
+    if (out.reach_max_depth) out.reach_max_depth[c] = (f & kCont) ? 1 : 0;
+    if (out.has_divergence) out.has_divergence[c] = (f & kNotDiv) ? 0 : 1;
+    if (out.energy) out.energy[c] = w.cand_e[c];
+    if (out.tree_depth) out.tree_depth[c] = w.tree_depth[c];
+  }
+}
+
 __global__ void nuts_finalize_kernel(NutsDev w, NutsOutputs out, int unrolled) {
+  const int c = warp_id(), lane = threadIdx.x & 31;
+  if (c >= w.C) return;
+  nuts_chain_finalize(w, c, lane, out, unrolled);
+}
+
+// --------------------------------------------------------------------------
+// Free-running NUTS: one leaf of every running chain per iteration.  The
+// per-chain bodies are the lock-step kernels'; the draws are addressed by the
+// chain's own transition key, depth and leaf, so a chain's transitions equal
+// the lock-step sampler's with the same keys.
+// --------------------------------------------------------------------------
+__global__ void nuts_free_start_kernel(NutsDev w, FreeDev f, const float* __restrict__ q,
+                                      const double* __restrict__ l,
+                                      const float* __restrict__ g) {
   const int c = warp_id(), lane = threadIdx.x & 31;
   if (c >= w.C) return;
   const size_t o = voff(w, c);
   const int D = vdim(w, c);
   for (int d = lane; d < D; d += 32) {
-    out.state[o + d] = w.cand_q[o + d];
-    out.grads[o + d] = w.cand_g[o + d];
+    w.cand_q[o + d] = q[o + d];
+    w.cand_g[o + d] = g[o + d];
   }
   if (lane == 0) {
-    const uint8_t f = w.flags[c];
-    out.target_log_prob[c] = w.cand_l[c];
-    out.log_accept_ratio[c] = log(w.eds[c] / (double)w.lf[c]);   // nuts.py:429-432
-    out.leapfrogs_taken[c] = w.lf[c] * unrolled;
-    out.is_accepted[c] = (f & kAccepted) ? 1 : 0;
-    out.reach_max_depth[c] = (f & kCont) ? 1 : 0;
-    out.has_divergence[c] = (f & kNotDiv) ? 0 : 1;
-    out.energy[c] = w.cand_e[c];
-    if (out.tree_depth) out.tree_depth[c] = w.tree_depth[c];
+    w.cand_l[c] = l[c];
+    f.t[c] = 0;
+    f.phase[c] = kPhaseStart;
+    w.flags[c] = f.kmax > 0 ? kRunning : 0;
   }
+}
+
+// Start the chain's transition and/or tree depth if due, then its leaf's
+// half kick + drift.
+__global__ void nuts_free_prepare_kernel(NutsDev w, FreeDev f) {
+  const int j = warp_id(), lane = threadIdx.x & 31;
+  if (j >= *w.act_count) return;
+  const int c = w.act_idx[j];
+  uint8_t ph = f.phase[c];
+  if (ph == kPhaseStart) {
+    const uint2 key = step_key(f.seed, f.first + (uint32_t)f.t[c]);
+    nuts_chain_init(w, c, lane, w.cand_q, w.cand_l, w.cand_g,
+                    eps_of(f.eps_in, f.eps_per_chain, c), key);
+    __syncwarp();
+    if (lane == 0) {
+      f.key[c] = key;
+      w.flags[c] |= kRunning;
+      f.depth[c] = 0;
+    }
+    ph = kPhaseDepth;
+  }
+  if (ph == kPhaseDepth) {
+    __syncwarp();
+    if (lane == 0) nuts_chain_depth_begin(w, c, f.key[c], f.depth[c]);
+    __syncwarp();
+    nuts_chain_zero_cumsum(w, c, lane);
+    if (lane == 0) {
+      f.leaf[c] = 0;
+      f.phase[c] = kPhaseLeaf;
+    }
+  }
+  __syncwarp();
+  nuts_chain_leaf_pre(w, c, j, lane);
+}
+
+// The leaf's bookkeeping; at the end of the chain's subtree the tree-level
+// step; at the end of its trajectory the transition's results go to the
+// trace and the chain's next transition is due.
+__global__ void nuts_free_post_kernel(NutsDev w, FreeDev f) {
+  const int j = warp_id(), lane = threadIdx.x & 31;
+  if (j >= *w.act_count) return;
+  const int c = w.act_idx[j];
+  const uint2 key = f.key[c];
+  const int depth = f.depth[c], leaf = f.leaf[c];
+  nuts_chain_leaf_post(w, c, j, lane, key, depth, leaf, f.wtab[leaf], f.rlo[leaf], f.rhi[leaf],
+                       f.max_energy_diff);
+  __syncwarp();
+  if ((w.flags[c] & kSubCont) && leaf + 1 < (1 << depth)) {
+    if (lane == 0) f.leaf[c] = leaf + 1;
+    return;
+  }
+  nuts_chain_depth_end(w, c, lane, key, depth);
+  __syncwarp();
+  if ((w.flags[c] & kCont) && depth + 1 < f.max_depth) {
+    if (lane == 0) {
+      f.depth[c] = depth + 1;
+      f.phase[c] = kPhaseDepth;
+    }
+    return;
+  }
+  const int t = f.t[c];
+  const size_t C = (size_t)w.C;
+  NutsOutputs out{f.tr_state ? f.tr_state + (size_t)t * f.tr_estride : nullptr,
+                  f.tr_logp ? f.tr_logp + (size_t)t * C : nullptr, nullptr,
+                  f.tr_lar ? f.tr_lar + (size_t)t * C : nullptr,
+                  f.tr_lf ? f.tr_lf + (size_t)t * C : nullptr,
+                  f.tr_acc ? f.tr_acc + (size_t)t * C : nullptr, nullptr,
+                  f.tr_div ? f.tr_div + (size_t)t * C : nullptr, nullptr, nullptr};
+  nuts_chain_finalize(w, c, lane, out, 1);
+  __syncwarp();
+  if (lane == 0) {
+    f.t[c] = t + 1;
+    f.phase[c] = kPhaseStart;
+    if (t + 1 >= f.kmax) w.flags[c] &= (uint8_t)~kRunning;
+  }
+}
+
+__global__ void nuts_free_done_kernel(FreeDev f, int C, int32_t* __restrict__ out) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < C) out[c] = f.t[c];
 }
 
 // --------------------------------------------------------------------------
@@ -697,7 +843,7 @@ static void nuts_eval(gbm_nuts* k, cudaStream_t s, bool capturing = false) {
     GBM_CUDA(cudaEventRecord(k->prof_events[k->prof_used], s));
   }
   k->target->impl->eval(w.qw, w.D, w.act_count, w.C, w.lw, w.gw, w.D, k->target_ws.ptr, s);
-  k->prof_launches += k->target->impl->launches_per_eval(w.C);
+  if (!capturing) k->prof_launches += k->target->impl->launches_per_eval(w.C);
   if (k->profiling && !capturing) {
     GBM_CUDA(cudaEventRecord(k->prof_events[k->prof_used + 1], s));
     k->prof_used += 2;
@@ -813,6 +959,120 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
   nuts_finalize_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, out, k->unrolled_leapfrog_steps);
   GBM_CUDA(cudaGetLastError());
   k->prof_launches += 2;
+}
+
+int64_t nuts_run_free(gbm_nuts* k, int64_t chains, const float* q, const double* l,
+                      const float* g, const float* eps, int eps_per_chain, uint2 seed,
+                      uint32_t first_step, int kmax, int64_t max_leaf_iterations, FreeDev f,
+                      int32_t* transitions_done) {
+  gbm_context* ctx = k->target->ctx;
+  cudaStream_t s = ctx->stream;
+  NutsDev w = k->dev;
+  w.C = (int)chains;
+  w.inv_mass = k->inv_mass;
+  w.im_per_chain = k->im_per_chain;
+  const int C = (int)chains;
+  const int leaves = 1 << k->max_tree_depth;
+  // Per-chain loop state and the leaf tables (device), carved from free_mem.
+  const size_t tab = ((size_t)leaves * 3 * sizeof(int) + 255) / 256 * 256;
+  const size_t per = ((size_t)C * (3 * sizeof(int) + sizeof(uint2) + 1) + 255) / 256 * 256;
+  if (k->free_mem.bytes < tab + per) {
+    GBM_CUDA(cudaStreamSynchronize(s));
+    k->free_mem.reserve(tab + per);
+  }
+  char* base = k->free_mem.as<char>();
+  int* tabs = reinterpret_cast<int*>(base);
+  std::vector<int> host_tab(3 * leaves);
+  std::copy(k->write_instr.begin(), k->write_instr.end(), host_tab.begin());
+  std::copy(k->read_lo.begin(), k->read_lo.end(), host_tab.begin() + leaves);
+  std::copy(k->read_hi.begin(), k->read_hi.end(), host_tab.begin() + 2 * leaves);
+  GBM_CUDA(cudaMemcpyAsync(tabs, host_tab.data(), sizeof(int) * 3 * leaves,
+                           cudaMemcpyHostToDevice, s));
+  GBM_CUDA(cudaStreamSynchronize(s));   // host_tab is freed on return
+  f.wtab = tabs;
+  f.rlo = tabs + leaves;
+  f.rhi = tabs + 2 * leaves;
+  char* pc = base + tab;
+  f.key = reinterpret_cast<uint2*>(pc);
+  f.t = reinterpret_cast<int*>(pc + sizeof(uint2) * C);
+  f.depth = f.t + C;
+  f.leaf = f.t + 2 * C;
+  f.phase = reinterpret_cast<uint8_t*>(f.t + 3 * C);
+  f.eps_in = eps;
+  f.eps_per_chain = eps_per_chain;
+  f.seed = seed;
+  f.first = first_step;
+  f.kmax = kmax;
+  f.max_depth = k->max_tree_depth;
+  f.max_energy_diff = k->max_energy_diff;
+  const int wb = warp_blocks(chains);
+  nuts_free_start_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, f, q, l, g);
+  GBM_CUDA(cudaGetLastError());
+  k->prof_launches += 1;
+  auto iteration = [&](cudaStream_t ls, bool capturing) {
+    build_active(w, kRunning, ls);
+    nuts_free_prepare_kernel<<<wb, 32 * kWarpsPerBlock, 0, ls>>>(w, f);
+    nuts_eval(k, ls, capturing);
+    nuts_free_post_kernel<<<wb, 32 * kWarpsPerBlock, 0, ls>>>(w, f);
+    GBM_CUDA(cudaGetLastError());
+    if (!capturing) k->prof_launches += 3;
+  };
+  // Batches of `batch` iterations, replayed as one CUDA graph (captured for
+  // this call: its pointers are the call's); the host polls the running count
+  // recorded after each batch, at most two batches behind the device.
+  const int batch = 8;
+  cudaGraphExec_t exec = nullptr;
+  const bool graphs = k->use_graphs && !k->profiling;
+  if (graphs) {
+    cudaGraph_t graph;
+    cudaStream_t cs = k->graph_stream;
+    GBM_CUDA(cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal));
+    for (int i = 0; i < batch; ++i) iteration(cs, true);
+    GBM_CUDA(cudaStreamEndCapture(cs, &graph));
+    GBM_CUDA(cudaGraphInstantiate(&exec, graph, 0));
+    GBM_CUDA(cudaGraphDestroy(graph));
+  }
+  int* host_flags = ctx->host_flags;
+  int64_t iters = 0;
+  int64_t b = 0;
+  try {
+    while (iters < max_leaf_iterations) {
+      const int64_t n = std::min<int64_t>(batch, max_leaf_iterations - iters);
+      if (exec && n == batch) {
+        GBM_CUDA(cudaGraphLaunch(exec, s));
+        k->prof_launches += (int64_t)batch * (3 + k->target->impl->launches_per_eval(C));
+      } else {
+        for (int64_t i = 0; i < n; ++i) iteration(s, false);
+      }
+      iters += n;
+      const int slot = (int)(b % 4);
+      GBM_CUDA(cudaMemcpyAsync(host_flags + 1 + slot, w.act_count, sizeof(int),
+                               cudaMemcpyDeviceToHost, s));
+      GBM_CUDA(cudaEventRecord(k->poll_events[slot], s));
+      if (b >= 1) {
+        const int prev = (int)((b - 1) % 4);
+        GBM_CUDA(cudaEventSynchronize(k->poll_events[prev]));
+        check_device_error(ctx);
+        // The running count of two batches ago bounds the work left: stop
+        // once no chain was running then.
+        if (host_flags[1 + prev] == 0) break;
+      }
+      ++b;
+    }
+  } catch (...) {
+    if (exec) cudaGraphExecDestroy(exec);
+    throw;
+  }
+  if (exec) {
+    GBM_CUDA(cudaStreamSynchronize(s));
+    GBM_CUDA(cudaGraphExecDestroy(exec));
+  }
+  if (transitions_done) {
+    nuts_free_done_kernel<<<(C + 255) / 256, 256, 0, s>>>(f, C, transitions_done);
+    GBM_CUDA(cudaGetLastError());
+  }
+  k->last_leaf_iterations = iters;
+  return iters;
 }
 
 void hmc_setup(gbm_hmc* k) {

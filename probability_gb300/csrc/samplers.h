@@ -17,6 +17,37 @@ enum ChainFlag : uint8_t {
   kSubCont = 8,     // current subtree still growing
   kSubNotDiv = 16,  // subtree-level not_divergence
   kForward = 32,    // direction of the current subtree
+  kRunning = 64,    // free-running loop: the chain has transitions left
+};
+
+// Free-running NUTS (every chain at its own transition, depth and leaf):
+// per-chain loop state on the device.
+enum FreePhase : uint8_t { kPhaseStart = 0, kPhaseDepth = 1, kPhaseLeaf = 2 };
+
+struct FreeDev {
+  int* t;                   // [C] transitions completed
+  int* depth;               // [C] tree depth of the current doubling
+  int* leaf;                // [C] leaf within the current subtree
+  uint8_t* phase;           // [C] FreePhase
+  uint2* key;               // [C] key of the current transition
+  const int* wtab;          // [2^max_depth] write slot per leaf (-1: none)
+  const int* rlo;           // [2^max_depth] U-turn read range per leaf
+  const int* rhi;
+  const float* eps_in;      // step size: [1] or [C]
+  int eps_per_chain;
+  uint2 seed;
+  uint32_t first;           // sample_chain step of each chain's transition 0
+  int kmax;                 // transitions per chain
+  int max_depth;
+  double max_energy_diff;
+  // Trace [kmax][...]; any may be NULL.
+  float* tr_state;          // [kmax][state elements]
+  double* tr_logp;          // [kmax][C]
+  double* tr_lar;
+  int32_t* tr_lf;
+  uint8_t* tr_acc;
+  uint8_t* tr_div;
+  size_t tr_estride;        // state elements per transition
 };
 
 // Device pointers of the NUTS workspace (passed to kernels by value).
@@ -142,6 +173,15 @@ void dual_averaging_update_reduced(cudaStream_t s, const double* reduced, int64_
 void dual_averaging_update(cudaStream_t s, const double* lar, int64_t C, int per_chain,
                            const DaParams& prm, const double* target_accept, double* state,
                            float* eps);
+// Free-running NUTS: each chain runs `kmax` transitions (keys step_key(seed,
+// first_step + t)) and starts its next transition as soon as its own tree
+// ends, so one long trajectory does not hold the others; at most
+// `max_leaf_iterations` leaf iterations.  Writes the trace and, per chain,
+// the transitions completed; returns the leaf iterations run.
+int64_t nuts_run_free(gbm_nuts* k, int64_t C, const float* q, const double* l, const float* g,
+                      const float* eps, int eps_per_chain, uint2 seed, uint32_t first_step,
+                      int kmax, int64_t max_leaf_iterations, FreeDev trace,
+                      int32_t* transitions_done);
 void nuts_sample_chain(gbm_nuts* k, int64_t C, float* q, double* l, float* g, float* eps,
                        int per_chain, uint2 seed, uint32_t first_step, int64_t num_results,
                        int64_t burnin, int64_t thin, const DaConfig& da, const ChainTrace& tr);
@@ -175,6 +215,7 @@ struct gbm_nuts {
   cudaStream_t graph_stream = nullptr;   // capture stream (graphs launch on the caller's)
   std::map<int64_t, cudaGraphExec_t> graphs;   // (chains, depth, first leaf)
   gbm::DeviceBuffer key_dev;   // uint2
+  gbm::DeviceBuffer free_mem;  // free-running loop: per-chain state and leaf tables
   int64_t graph_launches = 0;
   // Counters for the last transition (host-visible after one_step returns).
   int64_t last_leaf_iterations = 0;

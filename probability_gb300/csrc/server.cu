@@ -309,10 +309,9 @@ int gbm_server_submit(gbm_server* srv, const gbm_job_spec* spec, int64_t* job_id
   }
   if (s.family == GBM_FAMILY_LOGISTIC_REGRESSION &&
       (!s.x || !s.y || s.rows <= 0 || s.features < 1 || !(s.prior_scale > 0.f) ||
-       s.features > (s.precision == GBM_PRECISION_F32 ? 256 : 512) ||
        (s.precision == GBM_PRECISION_F32 && s.x_dtype != GBM_DTYPE_F32))) {
-    gbm::set_error("gbm_server_submit: logistic regression needs x, y, rows > 0 and features "
-                   "<= 256 (FP32) or <= 512 (mixed precision)");
+    gbm::set_error("gbm_server_submit: logistic regression needs x, y, rows > 0, features > 0, "
+                   "a positive prior scale and float32 X for FP32 precision");
     return GBM_EINVAL;
   }
   if (s.family == GBM_FAMILY_MVN && (!s.loc || !s.scale_tril_inv)) {

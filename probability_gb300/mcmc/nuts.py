@@ -7,6 +7,7 @@ precomputed U-turn slot tables, fused leapfrog + target gradient per leaf,
 multinomial sampling with float64 log-weights -- runs in the engine
 (``gbm_nuts_one_step``).  target_log_prob and energy are float64.
 """
+import collections
 import ctypes
 
 import numpy as np
@@ -56,6 +57,41 @@ def generate_efficient_write_read_instruction(instruction_array):
     else:
       read.append([0, 0])
   return write, np.asarray(read)
+
+
+FreeRun = collections.namedtuple(
+    'FreeRun', ['all_states', 'trace', 'transitions_done', 'leaf_iterations'])
+
+
+def run_free(handle, q, kr, step_size, per_chain, seed, first_step, transitions_per_chain,
+             max_leaf_iterations, state_shape):
+  """gbm_nuts_run_free for a sampler handle: q [elements] float32 on the
+  device, kr the results carrying target_log_prob / grads_target_log_prob.
+  Returns FreeRun(all_states [K, *state_shape], trace of [K, C] tensors,
+  transitions_done [C], leaf_iterations)."""
+  dev = q.device
+  C = kr.target_log_prob.numel()
+  K = int(transitions_per_chain)
+  E = q.numel()
+  tr = dict(target_log_prob=torch.empty((K, C), dtype=torch.float64, device=dev),
+            log_accept_ratio=torch.empty((K, C), dtype=torch.float64, device=dev),
+            leapfrogs_taken=torch.zeros((K, C), dtype=torch.int32, device=dev),
+            is_accepted=torch.zeros((K, C), dtype=torch.uint8, device=dev),
+            has_divergence=torch.zeros((K, C), dtype=torch.uint8, device=dev))
+  states = torch.empty((K, E), dtype=torch.float32, device=dev)
+  done = torch.empty(C, dtype=torch.int32, device=dev)
+  l0 = _util.as_tensor(kr.target_log_prob, torch.float64, dev).reshape(C).contiguous()
+  g0 = _util.as_tensor(kr.grads_target_log_prob, torch.float32, dev).reshape(-1).contiguous()
+  iters = ctypes.c_int64()
+  P = _native.ptr
+  _native.check(_native.lib().gbm_nuts_run_free(
+      handle, C, P(q), P(l0), P(g0), P(step_size), per_chain, _native.seed_words(seed),
+      int(first_step), K, int(max_leaf_iterations), P(done), P(states),
+      P(tr['target_log_prob']), P(tr['log_accept_ratio']), P(tr['leapfrogs_taken']),
+      P(tr['is_accepted']), P(tr['has_divergence']), ctypes.byref(iters)), 'gbm_nuts_run_free')
+  for k in ('is_accepted', 'has_divergence'):
+    tr[k] = tr[k].bool()
+  return FreeRun(states.reshape((K,) + tuple(state_shape)), tr, done, int(iters.value))
 
 
 class NoUTurnSampler(kernel_base.TransitionKernel):
@@ -148,6 +184,27 @@ class NoUTurnSampler(kernel_base.TransitionKernel):
         reach_max_depth=rmd.bool(), has_divergence=div.bool(), energy=energy,
         seed=_util.seed_tensor(seed))
     return unflat(nq), kr
+
+  def run_free(self, current_state, kernel_results, transitions_per_chain, seed,
+               first_step=0, max_leaf_iterations=1 << 40):
+    """Free-running transitions: every chain runs `transitions_per_chain`
+    one_step transitions with keys step_key(seed, first_step + t) (the
+    transitions sample_chain runs at a fixed step size), each chain starting
+    its next transition as soon as its own trajectory ends (no lock-step);
+    per chain equal to one_step with the same keys.  At most
+    `max_leaf_iterations` leapfrog steps per chain.  Returns
+    FreeRun(all_states [K, C, D], trace, transitions_done, leaf_iterations)."""
+    q, layout, is_list = _util.flatten_state(current_state)
+    if is_list:
+      raise NotImplementedError('run_free takes a single-part state')
+    C, D = q.shape
+    self._ensure(C)
+    eps, per_chain = _step_size_tensor(kernel_results.step_size, C, q.device)
+    run = run_free(self._handle, q.contiguous().reshape(-1), kernel_results, eps.contiguous(),
+                   per_chain, _util.sanitize_seed(seed), first_step, transitions_per_chain,
+                   max_leaf_iterations, (C, D))
+    self.last_leaf_iterations = run.leaf_iterations
+    return run
 
   def bootstrap_results(self, init_state):
     """nuts.py:456-503 (one gradient evaluation; energy uses unit momenta)."""

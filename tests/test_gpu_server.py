@@ -102,13 +102,32 @@ def test_server_admission_respects_budget(pg):
   srv.close()
 
 
+@pytest.mark.parametrize('d,precision', [(300, 'fp32'), (600, 'mixed')])
+def test_server_job_beyond_the_fused_kernels_feature_limits(pg, d, precision):
+  """Above 256 (FP32) or 512 (mixed) features a job runs on the library-GEMM
+  target and still equals the single-sampler path."""
+  from probability_gb300.serving import Server, DONE
+  srv = Server(workers=1, memory_budget_bytes=4 * 2**30)
+  job = _logreg_job(srv, seed=7, n=1500, d=d, chains=24, results=4, precision=precision)
+  assert job.wait()['status'] == DONE
+  X, y, _ = _problems.logreg_data(1500, d, seed=7, scale=1.0 / np.sqrt(d))
+  t = pg.LogisticRegression(X, y, precision=precision)
+  k = pg.mcmc.DualAveragingStepSizeAdaptation(
+      pg.mcmc.NoUTurnSampler(t, step_size=0.1, max_tree_depth=8), num_adaptation_steps=10,
+      target_accept_prob=0.8)
+  run = pg.mcmc.run_chain(k, 4, torch.from_numpy(_problems.init_state(24, d, seed=7)).cuda(),
+                          num_burnin_steps=5, seed=(7, 1))
+  assert torch.equal(job.states, run.all_states)
+  assert torch.equal(job.leapfrogs_taken, run.trace['leapfrogs_taken'])
+  srv.close()
+
+
 def test_server_rejects_bad_specs(pg):
   from probability_gb300.serving import Server
   srv = Server(workers=1, memory_budget_bytes=2**30)
-  X, y, _ = _problems.logreg_data(100, 600, seed=1)
-  with pytest.raises(ValueError):   # beyond the mixed path's 512 features
-    srv.submit_logistic_regression(X, y, np.zeros((4, 600), np.float32), 2)
-  with pytest.raises(ValueError):   # beyond the FP32 path's 256 features
-    srv.submit_logistic_regression(X[:, :300], y, np.zeros((4, 300), np.float32), 2,
-                                   precision='fp32')
+  X, y, _ = _problems.logreg_data(100, 6, seed=1)
+  with pytest.raises(ValueError):   # init_state width is not the feature count
+    srv.submit_logistic_regression(X, y, np.zeros((4, 5), np.float32), 2)
+  with pytest.raises(ValueError):   # the prior scale must be positive
+    srv.submit_logistic_regression(X, y, np.zeros((4, 6), np.float32), 2, prior_scale=0.0)
   srv.close()
