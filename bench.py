@@ -42,12 +42,14 @@ WORKLOADS = {
                                 num_adaptation_steps=1000, precision='fp32', start='laplace',
                                 step_size_draws=0.011),
 }
-# Mixed precision at scale: X 1e6 x 512 BF16, 4096 chains, NUTS depth 8.
+# Mixed precision at scale: X 1e6 x 512 BF16, 4096 chains, NUTS depth 8;
+# Laplace draws (Newton on the GPU), then --warm-in dual-averaging transitions
+# fix the step size of the timed draws.
 WORKLOADS['nuts_logreg_1e6x512_bf16'] = dict(n=1000000, d=512, chains=4096, depth=8, seed=2,
                                              feature_scale=512 ** -0.5, step0=0.01,
                                              target_accept=0.8, num_adaptation_steps=1000,
                                              precision='mixed', x_dtype='bf16',
-                                             precision_report=10000)
+                                             precision_report=10000, start='laplace_da')
 WORKLOADS['hmc_logreg_1000x25'] = dict(n=1000, d=25, chains=64, seed=0, feature_scale=1.0,
                                        step0=0.03, leapfrogs=10, burnin=500, precision='fp32')
 # Batched uneven posteriors: 128 multivariate normals, D ~ log-U[8, 2048],
@@ -578,6 +580,38 @@ def laplace_start(X, y, chains, seed, prior_scale=1.0, iters=25):
   return draws.astype(np.float32)
 
 
+def laplace_start_device(X_engine, y, chains, seed, dev, prior_scale=1.0, iters=30):
+  """laplace_start on the GPU in float64 (torch), for data too large for a
+  host Newton solve: the MAP by Newton's method on the engine's X (BF16
+  values where the workload stores BF16), then N(beta_MAP, H^-1) draws from
+  a seeded NumPy generator."""
+  import torch
+  X = X_engine.to(dev).to(torch.float64)
+  yv = torch.as_tensor(y, dtype=torch.float64, device=dev)
+  D = X.shape[1]
+  prec = 1.0 / prior_scale ** 2
+  eye = torch.eye(D, dtype=torch.float64, device=dev)
+  beta = torch.zeros(D, dtype=torch.float64, device=dev)
+
+  def hessian(b):
+    s = torch.sigmoid(X @ b)
+    return (X * (s * (1.0 - s))[:, None]).T @ X + prec * eye, s
+
+  for _ in range(iters):
+    H, s = hessian(beta)
+    g = X.T @ (yv - s) - prec * beta
+    step = torch.linalg.solve(H, g)
+    beta = beta + step
+    if float(step.abs().max()) < 1e-12:
+      break
+  H, _ = hessian(beta)
+  L = torch.linalg.cholesky(H)
+  zz = torch.from_numpy(np.random.default_rng(seed + 100).standard_normal((chains, D))).to(dev)
+  draws = beta + torch.linalg.solve_triangular(L.T, zz.T, upper=True).T   # cov = H^-1
+  del X
+  return draws.to(torch.float32).cpu().numpy()
+
+
 def draws_phase_keys(w, count):
   """Keys of the timed transitions: sample_chain's per-step keys (seed, 0)
   at steps num_adaptation_steps, num_adaptation_steps + 1, ... (the first
@@ -738,19 +772,27 @@ def split_rhat_max(pg, draws):
     return None
 
 
-def nuts_config(args, w, precision, world=1):
+def nuts_config(args, w, precision, world=1, eps=None):
+  start = w.get('start')
+  if start == 'laplace':
+    desc = ('Laplace approximation of the posterior (seeded), step size %g: the draws phase '
+            'after adaptation' % w['step_size_draws'])
+  elif start == 'laplace_da':
+    desc = ('Laplace approximation of the posterior (seeded, Newton on the GPU in float64), '
+            'then %d dual-averaging transitions; the timed transitions keep step size %s '
+            '(geometric mean of the second half), the draws phase after adaptation'
+            % (args.warm_in, '%.6g' % eps if eps else 'from the warm-in'))
+  else:
+    desc = '%d dual-averaging warm-in transitions from N(0, 0.1^2)' % args.warm_in
+  laplace = start in ('laplace', 'laplace_da')
   return {'workload': args.workload, 'rows': w['n'], 'features': w['d'],
           'chains': w['chains'], 'max_tree_depth': w['depth'],
           'target_accept_prob': w['target_accept'],
           'num_adaptation_steps': w['num_adaptation_steps'],
-          'precision': precision,
-          'start': ('Laplace approximation of the posterior (seeded), step size %g: the '
-                    'draws phase after adaptation' % w['step_size_draws']
-                    if w.get('start') == 'laplace' else
-                    '%d dual-averaging warm-in transitions from N(0, 0.1^2)' % args.warm_in),
+          'precision': precision, 'start': desc,
           'timed_transitions': 'keys of sample_chain steps %d.. (after %d warm-up steps)'
                                % (w['num_adaptation_steps'] + args.warmup, args.warmup)
-                               if w.get('start') == 'laplace' else 'after the warm-in',
+                               if laplace else 'after the warm-in',
           'l2': 'flushed between timed steps (256 MB write outside the step events)',
           'parallelism': 'single' if world == 1 else 'replicas x %d' % world}
 
@@ -767,13 +809,14 @@ def run_engine(args, w):
   from probability_gb300 import replicas
   dev = torch.device('cuda', local)
   X, y, init = make_data(w)
-  laplace = w.get('start') == 'laplace'
-  if laplace:
-    init = laplace_start(X, y, w['chains'], w['seed'])
-  if world > 1:  # independent replicas: per-rank initial state
-    init = replicas.replica_init(init.shape, w['seed'], rank) if not laplace else \
-        laplace_start(X, y, w['chains'], w['seed'] + 7919 * rank)
+  laplace = w.get('start') in ('laplace', 'laplace_da')
   X_engine = engine_features(X, w)
+  if laplace:
+    start_seed = w['seed'] + 7919 * rank
+    init = laplace_start(X, y, w['chains'], start_seed) if w['start'] == 'laplace' else \
+        laplace_start_device(X_engine, y, w['chains'], start_seed, dev)
+  elif world > 1:  # independent replicas: per-rank initial state
+    init = replicas.replica_init(init.shape, w['seed'], rank)
   precision = args.precision or w['precision']
   state0 = torch.from_numpy(init).to(dev)
   l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -794,7 +837,21 @@ def run_engine(args, w):
     return ks
 
   if laplace:
-    eps = w['step_size_draws']
+    eps = w.get('step_size_draws')
+    if w['start'] == 'laplace_da':
+      # Dual averaging from the Laplace draws; the timed transitions keep the
+      # geometric mean of the step sizes of its second half.
+      warm = Leg(pg, X_engine, y, w, precision, w['step0'], dev)
+      q = state0.clone()
+      kr = warm.kernel.bootstrap_results(q)
+      logs = []
+      for i in range(args.warm_in):
+        q, kr = warm.kernel.one_step(q, kr, seed=pg._util.step_key((w['seed'], 2), i))
+        if i >= args.warm_in // 2:
+          logs.append(float(torch.log(kr.new_step_size.reshape(-1)[0]).item()))
+      eps = float(np.exp(np.mean(logs)))
+      state0 = q
+      del warm, kr
     leg = Leg(pg, X_engine, y, w, precision, eps, dev)
     leg.prewarm(state0, args.prewarm, (w['seed'], 1))
     q, kr = leg.start(state0)
@@ -934,7 +991,7 @@ def run_engine(args, w):
         'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32' if precision == 'fp32' else 'bf16+f32',
         'data': 'synthetic (seeded numpy default_rng(%d))' % w['seed'],
-        'config': nuts_config(args, w, precision, world),
+        'config': nuts_config(args, w, precision, world, eps),
         'min_ess_per_s': ess_s,
         'split_rhat_max_timed_draws': rhat,
         'lane_grads_profiled_pass': {
@@ -1102,20 +1159,45 @@ def run_batch(args, w):
     t += 1
   torch.cuda.synchronize()
   ms0, ev0, la0 = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
-  _native.lib().gbm_nuts_read_profile(k._handle, ctypes.byref(ms0), ctypes.byref(ev0),
-                                      ctypes.byref(la0))
+  read_profile = lambda ms_, ev_, la_: _native.lib().gbm_nuts_read_profile(
+      k._handle, ctypes.byref(ms_), ctypes.byref(ev_), ctypes.byref(la_))
   flops_chain = torch.as_tensor(
       [2.0 * tt.event_dim ** 2 if isinstance(tt, pg.MultivariateNormalTriL)
        else 10.0 * tt.groups for tt, c in members for _ in range(c)], dtype=torch.float64,
       device=dev)
   l2_flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+  C, E = batch.chains, batch.elements
+  member_of_chain = torch.repeat_interleave(
+      torch.arange(len(members), device=dev),
+      torch.as_tensor(list(batch.member_chains), device=dev))
+
+  def member_ess(states, prefix):
+    """Sum over posteriors of the minimum (over coordinates) ESS of the
+    member's draws states[:prefix[m]] (rows: transitions, ragged state);
+    posteriors with fewer than 4 draws contribute 0."""
+    total, counted = 0.0, 0
+    for m in range(len(members)):
+      P = int(prefix[m])
+      if P < 4:
+        continue
+      e0_, n = int(batch.elem_begin[m]), batch.member_chains[m] * batch.member_dims[m]
+      x = states[:P, e0_:e0_ + n].reshape(P, batch.member_chains[m], batch.member_dims[m])
+      ess = pg.mcmc.effective_sample_size(x, filter_beyond_positive_pairs=True,
+                                          cross_chain_dims=1)
+      total += float(ess.min().item())
+      counted += 1
+    return total, counted
+
   clocks = ClockSampler(local)
   clocks.start()
+  # ---- lock-step leg: BatchedNoUTurnSampler.one_step, every chain of every
+  # posterior at the same tree depth and leaf ----
+  lock_steps = max(1, min(args.steps, args.lock_steps))
+  read_profile(ms0, ev0, la0)
   lf_total = torch.zeros((), dtype=torch.int64, device=dev)
-  flops = torch.zeros((), dtype=torch.float64, device=dev)
   draws, step_ms, leaves = [], 0.0, 0
   torch.cuda.synchronize()
-  for _ in range(args.steps):
+  for _ in range(lock_steps):
     l2_flush.zero_()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
@@ -1125,99 +1207,152 @@ def run_batch(args, w):
     t += 1
     leaves += k.last_leaf_iterations
     lf_total += kr.leapfrogs_taken.sum()
-    flops += (kr.leapfrogs_taken.to(torch.float64) * flops_chain).sum()
     draws.append(q)
     e1.synchronize()
     step_ms += e0.elapsed_time(e1)
   torch.cuda.synchronize()
+  ms1, ev1, la1 = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+  read_profile(ms1, ev1, la1)
+  lock_s = step_ms / 1000.0
+  lock_ess = None
+  if lock_steps >= 20:
+    lock_ess, _ = member_ess(torch.stack(draws), [lock_steps] * len(members))
+  del draws
+  lock = {'value': int(lf_total.item()) / lock_s, 'unit': 'grad-evals/s', 'steps': lock_steps,
+          'ms_per_step': step_ms / lock_steps, 'leaves_per_step': leaves / lock_steps,
+          'sum_min_ess_per_s': (lock_ess / lock_s) if lock_ess is not None else None,
+          'gpu_launches': int(la1.value),   # each read returns the count since the last
+          'transitions': 'BatchedNoUTurnSampler.one_step: each step runs until the longest '
+                         'trajectory of any chain ends (up to 1023 leaves at depth 10)'}
+  # ---- free-running leg (timed, the line's value): BatchedNoUTurnSampler
+  # .run_free with a fixed leaf-iteration budget; every chain starts its next
+  # transition (keys step_key(seed, t0 + i)) as soon as its own trajectory
+  # ends.  Only the leapfrogs of completed transitions count. ----
+  budget = args.free_leaves
+  kmax = args.free_transitions
+  t0 = t
+  ls0 = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+  read_profile(*ls0)
+  l2_flush.zero_()
+  torch.cuda.synchronize()
+  f0 = torch.cuda.Event(enable_timing=True)
+  f1 = torch.cuda.Event(enable_timing=True)
+  f0.record(batch.stream)
+  run = k.run_free(q, kr, kmax, (w['seed'], 0), first_step=t0, max_leaf_iterations=budget)
+  f1.record(batch.stream)
+  f1.synchronize()
+  torch.cuda.synchronize()
   clk = clocks.stop()
-  ms, ev, la = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
-  _native.lib().gbm_nuts_read_profile(k._handle, ctypes.byref(ms), ctypes.byref(ev),
-                                      ctypes.byref(la))
-  secs = step_ms / 1000.0
-  grad_evals = int(lf_total.item())
-  # ---- end to end: the same sampler call with the ragged state, its
-  # log-densities and gradients copied in from pinned host memory and back
-  # every step (a bounded number of further transitions) ----
+  ls1 = ctypes.c_double(), ctypes.c_int64(), ctypes.c_int64()
+  read_profile(*ls1)
+  secs = f0.elapsed_time(f1) / 1000.0
+  done = run.transitions_done.to(torch.int64)
+  lf_tr = run.trace['leapfrogs_taken'].to(torch.int64)             # [kmax, C], 0 past done
+  grad_evals = int(lf_tr.sum().item())
+  flops = float((lf_tr.sum(0).to(torch.float64) * flops_chain).sum().item())
+  prefix = torch.full((len(members),), 1 << 30, dtype=torch.int64, device=dev)
+  prefix = prefix.scatter_reduce(0, member_of_chain, done, reduce='amin').cpu().tolist()
+  ess_sum, ess_members = member_ess(run.all_states, prefix)
+  done_cpu = done.cpu().numpy()
+  free_stats = {'leaf_iteration_budget': budget, 'leaf_iterations': run.leaf_iterations,
+                'max_transitions_per_chain': kmax,
+                'transitions_per_chain': {'min': int(done_cpu.min()),
+                                          'median': float(np.median(done_cpu)),
+                                          'max': int(done_cpu.max())},
+                'chains_at_max_transitions': int((done_cpu >= kmax).sum()),
+                'member_common_prefix': {'min': int(min(prefix)), 'max': int(max(prefix))},
+                'ess_members_with_4_or_more_draws': ess_members}
+  del run
+  # ---- end to end: run_free with the ragged state, log-densities and
+  # gradients uploaded from pinned host memory, and each chain's last
+  # completed state and transition count read back, every call ----
   e2e = None
-  e2e_steps = min(args.steps, 5)
-  if e2e_steps > 0:
+  if args.steps > 0:
+    e2e_budget = min(budget, 2 * 1023)
+    e2e_k = 32
     h_q = q.cpu().pin_memory()
     h_l = kr.target_log_prob.cpu().pin_memory()
     h_g = kr.grads_target_log_prob.cpu().pin_memory()
-    lf_e = torch.zeros((), dtype=torch.int64, device=dev)
-    torch.cuda.synchronize()
-    f0 = torch.cuda.Event(enable_timing=True)
-    f1 = torch.cuda.Event(enable_timing=True)
-    f0.record(batch.stream)
-    for _ in range(e2e_steps):
+    h_out = torch.empty(E, dtype=torch.float32).pin_memory()
+    h_done = torch.empty(C, dtype=torch.int32).pin_memory()
+    elem_chain = torch.repeat_interleave(
+        torch.arange(C, device=dev),
+        torch.as_tensor(np.repeat(batch.member_dims, batch.member_chains), device=dev))
+    elem_idx = torch.arange(E, device=dev)
+
+    def e2e_call(seed_step):
       with torch.cuda.stream(batch.stream):
         dq = h_q.to(dev, non_blocking=True)
-        kr = kr._replace(target_log_prob=h_l.to(dev, non_blocking=True),
-                         grads_target_log_prob=h_g.to(dev, non_blocking=True))
-      q2, kr = k.one_step(dq, kr, seed=pg._util.step_key((w['seed'], 0), t))
-      t += 1
+        kr2 = kr._replace(target_log_prob=h_l.to(dev, non_blocking=True),
+                          grads_target_log_prob=h_g.to(dev, non_blocking=True))
+      r = k.run_free(dq, kr2, e2e_k, (w['seed'], 0), first_step=seed_step,
+                     max_leaf_iterations=e2e_budget)
       with torch.cuda.stream(batch.stream):
-        lf_e += kr.leapfrogs_taken.sum()
-        h_q.copy_(q2, non_blocking=True)
-        h_l.copy_(kr.target_log_prob, non_blocking=True)
-        h_g.copy_(kr.grads_target_log_prob, non_blocking=True)
+        d = r.transitions_done.to(torch.int64)
+        last = (d[elem_chain] - 1).clamp_min(0)
+        fin = torch.where(d[elem_chain] > 0, r.all_states[last, elem_idx], dq)
+        h_out.copy_(fin, non_blocking=True)
+        h_done.copy_(r.transitions_done, non_blocking=True)
+        lf = int(r.trace['leapfrogs_taken'].to(torch.int64).sum().item())
       batch.stream.synchronize()
-    f1.record(batch.stream)
-    f1.synchronize()
-    e2e_s = f0.elapsed_time(f1) / 1000.0
-    E, C = batch.elements, batch.chains
-    e2e = {'value': int(lf_e.item()) / e2e_s, 'unit': 'grad-evals/s',
-           'h2d_bytes_per_step': E * 8 + C * 8, 'd2h_bytes_per_step': E * 8 + C * 8,
-           'steps': e2e_steps,
-           'transitions': 'BatchedNoUTurnSampler.one_step with the ragged state, log-densities '
-                          'and gradients copied in from pinned host memory and back every step'}
-  ess_sum = None
-  if args.steps >= 20:
-    D = torch.stack(draws)                  # [steps, elements]
-    ess_sum = 0.0
-    for m in range(len(members)):
-      e0_, n = int(batch.elem_begin[m]), batch.member_chains[m] * batch.member_dims[m]
-      x = D[:, e0_:e0_ + n].view(args.steps, batch.member_chains[m], batch.member_dims[m])
-      ess = pg.mcmc.effective_sample_size(x, filter_beyond_positive_pairs=True,
-                                          cross_chain_dims=1)
-      ess_sum += float(ess.min().item())
-  achieved = float(flops.item()) / secs / 1e12
+      return lf
+
+    e2e_call(t0 + kmax)             # allocations for the trace outside the timed call
+    torch.cuda.synchronize()
+    g0 = torch.cuda.Event(enable_timing=True)
+    g1 = torch.cuda.Event(enable_timing=True)
+    g0.record(batch.stream)
+    lf_e = e2e_call(t0 + kmax + e2e_k)
+    g1.record(batch.stream)
+    g1.synchronize()
+    e2e_s = g0.elapsed_time(g1) / 1000.0
+    e2e = {'value': lf_e / e2e_s, 'unit': 'grad-evals/s',
+           'h2d_bytes_per_step': E * 8 + C * 8, 'd2h_bytes_per_step': E * 4 + C * 4,
+           'steps': 1, 'leaf_iteration_budget': e2e_budget,
+           'transitions': 'BatchedNoUTurnSampler.run_free (%d leaf iterations) with the ragged '
+                          'state, log-densities and gradients uploaded from pinned host memory '
+                          'and each chain\'s last completed state and transition count read '
+                          'back' % e2e_budget}
+  achieved = flops / secs / 1e12
   fp32_peak = 2 * 128 * 152 * 2.07e9 / 1e12     # FMA lanes x 2 flop x SMs x max clock
   cpu = None
   if not args.no_cpu_baseline:
-    budget = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '15'))
-    rate, passes, dt, pick = cpu_batch_gradient_rate(spec, budget)
+    budget_s = float(os.environ.get('GBM_CPU_BASELINE_SECONDS', '15'))
+    rate, passes, dt, pick = cpu_batch_gradient_rate(spec, budget_s)
     cpu = {'value': rate, 'unit': 'grad-evals/s', 'cores': os.cpu_count(), 'kind': 'port',
            'sample': '%d passes of the log-prob+gradient of 16 of the 256 posteriors with all '
                      'their chains (%.1f s; the NUTS leaf cost, no tree bookkeeping); NumPy '
                      'float64 oracle targets, BLAS threads = all cores' % (passes, dt)}
   line = {
       'metric': METRIC_BATCH,
-      'value': grad_evals / secs, 'unit': 'grad-evals/s', 'n_gpus': 1, 'steps': args.steps,
-      'warmup': args.warmup, 'ms_per_step': step_ms / args.steps, 'higher_is_better': True,
+      'value': grad_evals / secs, 'unit': 'grad-evals/s', 'n_gpus': 1, 'steps': 1,
+      'warmup': args.warmup, 'ms_per_step': secs * 1000.0, 'higher_is_better': True,
       'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32 (f64 energies)',
       'data': 'synthetic (seeded numpy default_rng(%d))' % w['seed'],
       'config': {'workload': args.workload, 'posteriors': len(members),
                  'mvn_dims': [int(tt.event_dim) for tt, _ in members[:w['mvn']]],
-                 'chains_total': batch.chains, 'state_elements': batch.elements,
+                 'chains_total': C, 'state_elements': E,
                  'max_tree_depth': w['depth'], 'warm_in_transitions': args.warm_in,
                  'step_size': 'one per posterior, dual averaging (target %.2f) in the warm-in'
                               % w['target_accept'],
                  'preconditioned': bool(args.precondition),
                  'chain_tile_schedule': batch.schedule(),
-                 'l2': 'flushed between timed steps (256 MB write outside the step events)'},
-      'sum_min_ess_per_s': (ess_sum / secs) if ess_sum is not None else None,
-      'leaves_per_step': leaves / args.steps,
+                 'timed': 'one free-running call (BatchedNoUTurnSampler.run_free) of %d leaf '
+                          'iterations after %d lock-step warm-up and %d timed lock-step '
+                          'transitions' % (budget, args.warmup, lock_steps),
+                 'l2': 'flushed before each timed call (256 MB write outside the events)'},
+      'sum_min_ess_per_s': ess_sum / secs,
+      'free_running': free_stats,
+      'lock_step': lock,
       'roofline': {'bound': 'fp32', 'achieved': achieved, 'peak': fp32_peak, 'unit': 'TFLOP/s',
                    'frac': achieved / fp32_peak, 'traffic': None,
-                   'kernel': 'batch_phase_kernel (whole sampler step timed)',
+                   'kernel': 'batch_phase_kernel (whole free-running call timed; flops of '
+                             'completed transitions only)',
                    'peak_source': 'nominal FP32 FMA rate at the maximum SM clock'},
-      'setup_s': setup_s, 'gpu_launches': int(la.value), 'clocks': clk,
+      'setup_s': setup_s, 'gpu_launches': int(ls1[2].value), 'clocks': clk,
       'cpu_baseline': cpu, 'e2e': e2e,
   }
   print(json.dumps(line), flush=True)
-
 
 def serve_stream(pg, srv, jobs_spec, inputs, w, host):
   """Replay the stream through the job server.  host=False: each job's X, y
@@ -1301,15 +1436,23 @@ def run_serving(args, w):
   queue = np.array([i['start_s'] - i['submit_s'] for i in infos])
   busy = max(i['end_s'] for i in infos) - min(i['submit_s'] for i in infos)
   ess_sum, lf_sum, flops = 0.0, 0, 0.0
-  for js, h in zip(jobs_spec, handles):
+  per_job = []
+  for js, h, inf in zip(jobs_spec, handles, infos):
     st = h.states                       # [draws, C, D]
     lf = int(h.leapfrogs_taken.sum().item())
     lf_sum += lf
     flops += 4.0 * js['n'] * js['d'] * lf
+    ess_j = None
     if st.shape[0] >= 4:
       ess = pg.mcmc.effective_sample_size(st, filter_beyond_positive_pairs=True,
                                           cross_chain_dims=1)
-      ess_sum += float(ess.min().item())
+      ess_j = float(ess.min().item())
+      ess_sum += ess_j
+    run_s = inf['end_s'] - inf['start_s']
+    per_job.append([js['n'], js['d'], js['c'], js['draws'],
+                    round(lf / (js['c'] * js['draws']), 1), round(run_s, 2),
+                    round(4.0 * js['n'] * js['d'] * lf / run_s / 1e12, 1) if run_s > 0 else None,
+                    round(ess_j, 1) if ess_j is not None else None])
   value = ess_sum / busy
   del handles
   e2e = None
@@ -1379,6 +1522,9 @@ def run_serving(args, w):
       'queue_s': {'p50': float(np.percentile(queue, 50)), 'p99': float(np.percentile(queue, 99))},
       'makespan_s': busy, 'wall_s': wall, 'jobs_per_s': R / busy,
       'grad_evals_per_s': lf_sum / busy,
+      'jobs': {'columns': ['rows', 'features', 'chains', 'draws', 'leapfrogs per chain and draw',
+                           'run_s (adaptation + draws)', 'TFLOP/s of the draws over run_s',
+                           'min_ess'], 'rows': per_job},
       'e2e': e2e, 'roofline': roofline, 'cpu_baseline': cpu,
       'clocks': clk,
   }
@@ -1409,6 +1555,12 @@ def main():
                   help='time the batched log-prob+gradient alone (profiling aid)')
   ap.add_argument('--precondition', action='store_true',
                   help='nuts_batch_256: learn a diagonal metric per posterior in the warm-in')
+  ap.add_argument('--lock-steps', type=int, default=20,
+                  help='nuts_batch_256: timed lock-step transitions beside the free-running call')
+  ap.add_argument('--free-leaves', type=int, default=10230,
+                  help='nuts_batch_256: leaf-iteration budget of the timed free-running call')
+  ap.add_argument('--free-transitions', type=int, default=256,
+                  help='nuts_batch_256: transitions per chain at most in the free-running call')
   ap.add_argument('--kernel-rows', type=int, default=0,
                   help='with --kernel-only: rows of X (default: the workload\'s)')
   args = ap.parse_args()

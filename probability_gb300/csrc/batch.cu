@@ -14,11 +14,11 @@
 // tile list built on the device each leaf:
 //   schedule: for each member, its active chains are a contiguous run of the
 //             (sorted) active list; MVN members contribute
-//             ceil(active / ct) x ceil(D / 64) tiles, hierarchical members
+//             ceil(active / ct) x ceil(D / 128) tiles, hierarchical members
 //             ceil(active / 8) tiles.
-//   phase 0:  MVN tiles form u = L^-1 (x - loc) for a block of 64 rows of u
+//   phase 0:  MVN tiles form u = L^-1 (x - loc) for a block of 128 rows of u
 //             and that block's |u|^2; hierarchical tiles do all their work.
-//   phase 1:  MVN tiles form grad = -L^-T u for a block of 64 columns; the
+//   phase 1:  MVN tiles form grad = -L^-T u for a block of 128 columns; the
 //             column-block-0 tile also sums the |u|^2 blocks (fixed order).
 // Each CTA walks the list with a stride of the grid, so large and small
 // members share the machine in one launch.  The chain-tile width ct (32 or
@@ -38,8 +38,8 @@ namespace {
 
 enum BatchFamily : int { kBatchMvn = 1, kBatchHier = 2 };   // the GBM_FAMILY_* values
 
-constexpr int kOB = 64;          // rows / columns of u or grad per MVN tile
-constexpr int kKc = 32;          // K chunk
+constexpr int kOB = 128;         // rows / columns of u or grad per MVN tile
+constexpr int kKc = 16;          // K chunk
 constexpr int kThreads = 256;
 constexpr int kHierChains = 8;   // chains per hierarchical tile (a warp each)
 constexpr int kClasses = 4;      // size classes of D for the tile autotuner
@@ -116,25 +116,34 @@ __global__ void batch_schedule_kernel(const BDesc* __restrict__ d, int T,
   }
 }
 
-struct TileSmem {
-  float As[kKc][kOB + 4];   // [k][chain]
-  float Bs[kKc][kOB + 4];   // [k][output]
-  double red[16][kOB];
-  long long cof[kOB];
-  int cid[kOB];
+struct alignas(16) TileSmem {
+  float As[2][kKc][64 + 4];     // [stage][k][chain]
+  float Bs[2][kKc][kOB + 4];    // [stage][k][output]
+  double red[16][64];
+  long long cof[64];
+  int cid[64];
 };
 
-// One MVN tile: chains act[a0 .. a0 + nc) (nc <= CT) x outputs [o0, o0 + 64).
+// One MVN tile: chains act[a0 .. a0 + nc) (nc <= CT) x outputs [o0, o0 + 128).
 //   PHASE 0: U[c][o] = sum_{k <= o} (x_c[k] - loc[k]) L^-1[o][k]; |U_c|^2 over
 //            the block -> part.
 //   PHASE 1: G[c][o] = -sum_{k >= o} U_c[k] L^-1[k][o]; block 0 also writes
 //            logp = -1/2 sum of the |U|^2 blocks + log_norm.
+// Thread (ty, tx) of the 16 x 16 layout accumulates chains ty*CPT .. +CPT-1
+// and outputs tx*4 .. +3 and 64 + tx*4 .. +3 in registers (each K step: one
+// shared load of the chains, two conflict-free 16-byte loads of the outputs,
+// 8·CPT FMAs).  K chunks of 16 are double-buffered in shared memory: the
+// next chunk's global loads are issued into registers before the current
+// chunk's FMAs and stored to the other stage after them.
 template <int PHASE, int CT>
 __device__ void mvn_tile(const BDesc& d, const int* __restrict__ act, int a0, int nc, int ob,
                          const int64_t* __restrict__ coff, const float* __restrict__ X,
                          float* __restrict__ out, double* __restrict__ part,
                          double* __restrict__ logp, TileSmem& sm) {
-  constexpr int CPT = CT / 16;   // chains per thread
+  constexpr int CPT = CT / 16;                  // chains per thread (4 or 2)
+  constexpr int AL = kKc * CT / kThreads;       // A values each thread loads per chunk
+  constexpr int BL = kKc * kOB / kThreads;      // B values each thread loads per chunk
+  static_assert(AL >= 1 && BL >= 1, "tile loads");
   const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
   const int D = d.dim, o0 = ob * kOB;
   const float* M = d.linv;
@@ -145,45 +154,83 @@ __device__ void mvn_tile(const BDesc& d, const int* __restrict__ act, int a0, in
     sm.cof[tid] = c >= 0 ? coff[c] : 0;
   }
   __syncthreads();
-  float acc[CPT][4];
+  float acc[CPT][8];
 #pragma unroll
   for (int i = 0; i < CPT; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = 0.f;
+    for (int j = 0; j < 8; ++j) acc[i][j] = 0.f;
   const int k_begin = PHASE == 0 ? 0 : (o0 / kKc) * kKc;
   const int k_end = PHASE == 0 ? min(D, o0 + kOB) : D;
-  for (int k0 = k_begin; k0 < k_end; k0 += kKc) {
-    for (int i = tid; i < kKc * CT; i += kThreads) {
-      const int kk = i % kKc, cc = i / kKc, k = k0 + kk;
+  const int chunks = (k_end - k_begin + kKc - 1) / kKc;
+  float ra[AL], rb[BL];
+  // Chunk loads: A(k, chain) with k fastest (a chain's state is contiguous);
+  // B(k, o) = M[o][k] (phase 0, k fastest) or M[k][o] (phase 1, o fastest).
+  auto load = [&](int k0) {
+#pragma unroll
+    for (int r = 0; r < AL; ++r) {
+      const int i = tid + r * kThreads, kk = i % kKc, cc = i / kKc, k = k0 + kk;
       float v = 0.f;
       if (cc < nc && k < D) {
         v = X[sm.cof[cc] + k];
         if (PHASE == 0) v -= d.loc[k];
       }
-      sm.As[kk][cc] = v;
+      ra[r] = v;
     }
-    for (int i = tid; i < kKc * kOB; i += kThreads) {
-      if (PHASE == 0) {      // B(k, o) = M[o][k], k contiguous
+#pragma unroll
+    for (int r = 0; r < BL; ++r) {
+      const int i = tid + r * kThreads;
+      if (PHASE == 0) {
         const int kk = i % kKc, oo = i / kKc, k = k0 + kk, o = o0 + oo;
-        sm.Bs[kk][oo] = (o < D && k < D && k <= o) ? M[(size_t)o * D + k] : 0.f;
-      } else {               // B(k, o) = M[k][o], o contiguous
+        rb[r] = (o < D && k < D && k <= o) ? M[(size_t)o * D + k] : 0.f;
+      } else {
         const int oo = i % kOB, kk = i / kOB, k = k0 + kk, o = o0 + oo;
-        sm.Bs[kk][oo] = (o < D && k < D && k >= o) ? M[(size_t)k * D + o] : 0.f;
+        rb[r] = (o < D && k < D && k >= o) ? M[(size_t)k * D + o] : 0.f;
       }
     }
-    __syncthreads();
-#pragma unroll 8
+  };
+  auto store = [&](int st) {
+#pragma unroll
+    for (int r = 0; r < AL; ++r) {
+      const int i = tid + r * kThreads;
+      sm.As[st][i % kKc][i / kKc] = ra[r];
+    }
+#pragma unroll
+    for (int r = 0; r < BL; ++r) {
+      const int i = tid + r * kThreads;
+      if (PHASE == 0)
+        sm.Bs[st][i % kKc][i / kKc] = rb[r];
+      else
+        sm.Bs[st][i / kOB][i % kOB] = rb[r];
+    }
+  };
+  if (chunks > 0) {
+    load(k_begin);
+    store(0);
+  }
+  __syncthreads();
+  for (int ch = 0; ch < chunks; ++ch) {
+    const int st = ch & 1;
+    const bool more = ch + 1 < chunks;
+    if (more) load(k_begin + (ch + 1) * kKc);
+#pragma unroll
     for (int kk = 0; kk < kKc; ++kk) {
       float aa[CPT];
-#pragma unroll
-      for (int i = 0; i < CPT; ++i) aa[i] = sm.As[kk][ty * CPT + i];
-      const float4 b4 = *reinterpret_cast<const float4*>(&sm.Bs[kk][tx * 4]);
-      const float bb[4] = {b4.x, b4.y, b4.z, b4.w};
+      if (CPT == 4) {
+        const float4 a4 = *reinterpret_cast<const float4*>(&sm.As[st][kk][ty * 4]);
+        aa[0] = a4.x; aa[1] = a4.y; aa[CPT > 2 ? 2 : 0] = a4.z; aa[CPT > 3 ? 3 : 0] = a4.w;
+      } else {
+        const float2 a2 = *reinterpret_cast<const float2*>(&sm.As[st][kk][ty * 2]);
+        aa[0] = a2.x; aa[1] = a2.y;
+      }
+      const float4 b0 = *reinterpret_cast<const float4*>(&sm.Bs[st][kk][tx * 4]);
+      const float4 b1 = *reinterpret_cast<const float4*>(&sm.Bs[st][kk][64 + tx * 4]);
+      const float bb[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
 #pragma unroll
       for (int i = 0; i < CPT; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fmaf(aa[i], bb[j], acc[i][j]);
+        for (int j = 0; j < 8; ++j) acc[i][j] = fmaf(aa[i], bb[j], acc[i][j]);
     }
+    if (more) store(st ^ 1);
     __syncthreads();
   }
 #pragma unroll
@@ -191,8 +238,8 @@ __device__ void mvn_tile(const BDesc& d, const int* __restrict__ act, int a0, in
     const int cc = ty * CPT + i;
     double sq = 0.0;
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int o = o0 + tx * 4 + j;
+    for (int j = 0; j < 8; ++j) {
+      const int o = o0 + (j < 4 ? tx * 4 + j : 64 + tx * 4 + j - 4);
       if (cc < nc && o < D) {
         const float v = PHASE == 0 ? acc[i][j] : -acc[i][j];
         out[sm.cof[cc] + o] = v;
@@ -255,7 +302,7 @@ __device__ void hier_tile(const BDesc& d, const int* __restrict__ act, int a0, i
 }
 
 template <int PHASE>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, 2)
 batch_phase_kernel(const BDesc* __restrict__ desc, int T, const int* __restrict__ act,
                    const int* __restrict__ a, const int* __restrict__ na,
                    const int* __restrict__ base, const int64_t* __restrict__ coff,
@@ -367,7 +414,14 @@ class BatchTarget final : public Target {
     part_.reserve(sizeof(double) * (size_t)std::max<int64_t>(parts, 1));
     sched_.reserve(sizeof(int) * (size_t)(6 * (T_ + 1)));
     all_.reserve(sizeof(int) * (size_t)(C_ + 1));
-    grid_ = 4 * ctx->num_sms;
+    // Persistent CTAs: as many as are resident at once (a second wave would
+    // start its share of the tile list late).
+    int occ0 = 0, occ1 = 0;
+    GBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ0, batch_phase_kernel<0>,
+                                                           kThreads, 0));
+    GBM_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ1, batch_phase_kernel<1>,
+                                                           kThreads, 0));
+    grid_ = std::max(1, std::min(occ0, occ1)) * ctx->num_sms;
     upload();
     GBM_CUDA(cudaStreamSynchronize(ctx->stream));
     autotune();
