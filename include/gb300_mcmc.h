@@ -285,6 +285,19 @@ GBM_API int gbm_nuts_set_profiling(gbm_nuts* kernel, int enable);
  * same bits as per-leaf launches.  No reference counterpart: tfp.mcmc runs
  * under tf.function/XLA, which this replaces. */
 GBM_API int gbm_nuts_set_graphs(gbm_nuts* kernel, int enable);
+/* Free-running draws in gbm_nuts_sample_chain (off by default): the results
+ * whose transitions all run at the final step size (dual averaging past its
+ * window, or no adaptation) and no thinning come from the free-running loop
+ * of gbm_nuts_run_free -- per chain the same transitions (keys, step size,
+ * trace rows, streaming moments, final state), but no chain waits for the
+ * batch's longest trajectory.  The dual-averaging state then advances with
+ * every transition's accept ratio in order, as in lock-step.  For targets
+ * whose per-chain arithmetic does not depend on which chains are evaluated
+ * together (the multivariate-normal and hierarchical families) the results
+ * are bit-equal to lock-step; the logistic-regression kernels' row splits
+ * depend on the active-chain count, so there they agree to rounding.  No
+ * reference counterpart (tfp.mcmc runs every chain in lock-step). */
+GBM_API int gbm_nuts_set_free_running(gbm_nuts* kernel, int enable);
 /* Streaming moments on the device (for the running potential scale
  * reduction of experimental/mcmc/potential_scale_reduction_reducer.py and
  * diagnostic.py:476-568 without storing draws): fold one state of

@@ -60,6 +60,7 @@ _SIGNATURES = {
                           [ctypes.POINTER(I64)], ctypes.c_int),
     'gbm_nuts_set_profiling': ([P, ctypes.c_int], ctypes.c_int),
     'gbm_nuts_set_graphs': ([P, ctypes.c_int], ctypes.c_int),
+    'gbm_nuts_set_free_running': ([P, ctypes.c_int], ctypes.c_int),
     'gbm_moments_update': ([P, P, I64, I64, P, P], ctypes.c_int),
     'gbm_autocov_update': ([P, P, I64, I64, I32, P, P, P, P, P], ctypes.c_int),
     'gbm_nuts_set_inverse_mass': ([P, P, ctypes.c_int], ctypes.c_int),

@@ -644,6 +644,12 @@ int gbm_nuts_set_graphs(gbm_nuts* k, int enable) {
   return GBM_OK;
 }
 
+int gbm_nuts_set_free_running(gbm_nuts* k, int enable) {
+  if (!k) return invalid("gbm_nuts_set_free_running: NULL argument");
+  k->free_draws = enable != 0;
+  return GBM_OK;
+}
+
 int gbm_nuts_set_inverse_mass(gbm_nuts* k, const float* inverse_mass, int per_chain) {
   if (!k) return invalid("gbm_nuts_set_inverse_mass: NULL kernel");
   if (k->dev.ragged && inverse_mass && !per_chain)

@@ -6,6 +6,8 @@
 // into several calls (first_step advancing) draws exactly as one long run.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+#include <cstdint>
 #include <utility>
 
 #include "rng.cuh"
@@ -128,8 +130,23 @@ void nuts_sample_chain(gbm_nuts* k, int64_t C, float* q, double* l, float* g, fl
   float *cq = q, *cg = g, *nq = b.q, *ng = b.g;
   double *cl = l, *nl = b.l;
   const int64_t groups = per_chain ? C : 1;
+  // With free_draws, the results whose transitions all run at the final step
+  // size (dual averaging past its window, or none) come from the
+  // free-running loop: row r_free onward (no thinning).
+  int64_t r_free = num_results;
+  if (k->free_draws && thin == 0 && !k->dev.ragged && k->unrolled_leapfrog_steps == 1 &&
+      num_results > 0) {
+    int64_t adapt_end = 0;   // first transition of this call past the window
+    if (da.enabled) {
+      double step0 = 0.0;   // the window counter (state[3]) at the call's start
+      GBM_CUDA(cudaMemcpyAsync(&step0, da.state + 3, sizeof(double), cudaMemcpyDeviceToHost, s));
+      GBM_CUDA(cudaStreamSynchronize(s));
+      adapt_end = std::max<int64_t>(0, (int64_t)da.prm.num_adaptation_steps - (int64_t)step0);
+    }
+    r_free = std::min<int64_t>(num_results, std::max<int64_t>(0, adapt_end - burnin));
+  }
   uint32_t t = first_step;
-  for (int64_t r = 0; r < num_results; ++r) {
+  for (int64_t r = 0; r < r_free; ++r) {
     const int64_t n = (r == 0) ? 1 + burnin : 1 + thin;
     for (int64_t i = 0; i < n; ++i, ++t) {
       NutsOutputs out{nq, nl, ng, b.lar, b.lf, b.acc, b.rmd, b.div, b.energy, nullptr};
@@ -148,6 +165,57 @@ void nuts_sample_chain(gbm_nuts* k, int64_t C, float* q, double* l, float* g, fl
     copy_row(tr.has_divergence ? tr.has_divergence + r * C : nullptr, b.div, C, s);
     copy_row(tr.step_size ? tr.step_size + r * groups : nullptr, eps, groups, s);
     moments_update(s, cq, vec, r, tr.moment_mean, tr.moment_m2);
+  }
+  if (r_free < num_results) {
+    // Rows r_free .. num_results - 1 come from transitions burnin + r_free ..
+    // of this call.  With r_free == 0 the burn-in transitions that precede
+    // row 0 have not run yet: they run here, in lock-step.
+    if (r_free == 0 && burnin > 0) {
+      for (int64_t i = 0; i < burnin; ++i, ++t) {
+        NutsOutputs out{nq, nl, ng, b.lar, b.lf, b.acc, b.rmd, b.div, b.energy, nullptr};
+        nuts_one_step(k, C, cq, cl, cg, eps, per_chain, step_key(seed, t), out);
+        if (da.enabled)
+          dual_averaging_update(s, b.lar, C, per_chain, da.prm, da.target_accept, da.state, eps);
+        std::swap(cq, nq);
+        std::swap(cl, nl);
+        std::swap(cg, ng);
+      }
+    }
+    const int64_t K = num_results - r_free;
+    double* lar = tr.log_accept_ratio ? tr.log_accept_ratio + r_free * C : nullptr;
+    if (!lar && da.enabled) {   // the window counter and error sum follow every transition
+      k->free_lar.reserve(sizeof(double) * (size_t)(K * C));
+      lar = k->free_lar.as<double>();
+    }
+    FreeDev f{};
+    f.tr_state = tr.state ? tr.state + r_free * vec : nullptr;
+    f.tr_logp = tr.target_log_prob ? tr.target_log_prob + r_free * C : nullptr;
+    f.tr_lar = lar;
+    f.tr_lf = tr.leapfrogs_taken ? tr.leapfrogs_taken + r_free * C : nullptr;
+    f.tr_acc = tr.is_accepted ? tr.is_accepted + r_free * C : nullptr;
+    f.tr_div = tr.has_divergence ? tr.has_divergence + r_free * C : nullptr;
+    f.tr_estride = vec;
+    f.mom_mean = tr.moment_mean;
+    f.mom_m2 = tr.moment_m2;
+    f.mom_base = r_free;
+    nuts_run_free(k, C, cq, cl, cg, eps, per_chain, seed, t, (int)K, INT64_MAX, f, nullptr);
+    t += (uint32_t)K;
+    // Each chain's last transition is its final state.
+    const NutsDev& w = k->dev;
+    copy_row(q, w.cand_q, vec, s);
+    copy_row(g, w.cand_g, vec, s);
+    copy_row(l, w.cand_l, C, s);
+    cq = q;
+    cl = l;
+    cg = g;
+    // Dual averaging past its window keeps the step size; its counter and
+    // error sum advance with every transition's accept ratio, in order.
+    for (int64_t r = 0; r < K; ++r) {
+      if (da.enabled)
+        dual_averaging_update(s, lar + r * C, C, per_chain, da.prm, da.target_accept, da.state,
+                              eps);
+      copy_row(tr.step_size ? tr.step_size + (r_free + r) * groups : nullptr, eps, groups, s);
+    }
   }
   if (cq != q) {  // the final state lives in the scratch buffers: hand it back
     copy_row(q, cq, vec, s);

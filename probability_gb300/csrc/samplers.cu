@@ -508,6 +508,18 @@ __global__ void nuts_free_post_kernel(NutsDev w, FreeDev f) {
                   f.tr_acc ? f.tr_acc + (size_t)t * C : nullptr, nullptr,
                   f.tr_div ? f.tr_div + (size_t)t * C : nullptr, nullptr, nullptr};
   nuts_chain_finalize(w, c, lane, out, 1);
+  if (f.mom_mean) {   // as moments_update_kernel, with this chain's draw count
+    const size_t o = voff(w, c);
+    const int D = vdim(w, c);
+    const double inv_count = 1.0 / (double)(f.mom_base + t + 1);
+    for (int d = lane; d < D; d += 32) {
+      const double v = (double)w.cand_q[o + d];
+      const double delta = v - f.mom_mean[o + d];
+      const double mnew = f.mom_mean[o + d] + delta * inv_count;
+      f.mom_mean[o + d] = mnew;
+      f.mom_m2[o + d] += delta * (v - mnew);
+    }
+  }
   __syncwarp();
   if (lane == 0) {
     f.t[c] = t + 1;

@@ -47,6 +47,11 @@ struct FreeDev {
   int32_t* tr_lf;
   uint8_t* tr_acc;
   uint8_t* tr_div;
+  // Streaming moments (Welford, float64 [C][D]) of each chain's results:
+  // transition t of a chain is draw mom_base + t of its running mean / M2.
+  double* mom_mean;
+  double* mom_m2;
+  int64_t mom_base;
   size_t tr_estride;        // state elements per transition
 };
 
@@ -216,6 +221,11 @@ struct gbm_nuts {
   std::map<int64_t, cudaGraphExec_t> graphs;   // (chains, depth, first leaf)
   gbm::DeviceBuffer key_dev;   // uint2
   gbm::DeviceBuffer free_mem;  // free-running loop: per-chain state and leaf tables
+  // sample_chain runs the draws after adaptation (fixed step size, no
+  // thinning) free-running: per chain the same transitions, without waiting
+  // for the batch's longest trajectory.
+  bool free_draws = false;
+  gbm::DeviceBuffer free_lar;  // log-accept ratios of a free segment when none are traced
   int64_t graph_launches = 0;
   // Counters for the last transition (host-visible after one_step returns).
   int64_t last_leaf_iterations = 0;

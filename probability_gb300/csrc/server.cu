@@ -80,6 +80,10 @@ size_t estimate_bytes(const gbm_job_spec& s, int num_sms) {
   b += 4.0 * vec * (14.0 + 2.0 * s.max_tree_depth) + 160.0 * C;   // NUTS workspace
   b += 8.0 * vec + 64.0 * C;                                        // chain loop buffers
   b += 8.0 * vec + 16.0 * C;                                        // job state
+  // Free-running draws: leaf tables, per-chain loop state and, when the job
+  // traces no log-accept ratios, their rows for the dual-averaging replay.
+  b += 12.0 * (double)(1 << s.max_tree_depth) + 32.0 * C;
+  if (!s.trace_log_accept_ratio) b += 8.0 * C * (double)s.num_results;
   return (size_t)b + (1u << 20);
 }
 
@@ -139,6 +143,7 @@ void run_job(gbm_context* ctx, Job* job) {
   k.max_tree_depth = s.max_tree_depth;
   k.max_energy_diff = 1000.0;
   k.unrolled_leapfrog_steps = 1;
+  k.free_draws = true;   // draws after adaptation: no chain waits for another's trajectory
   nuts_setup(&k);
   DeviceBuffer q, l, g, eps, da;
   q.reserve(sizeof(float) * C * D);

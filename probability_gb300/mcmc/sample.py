@@ -65,10 +65,15 @@ def _unwrap(kernel):
 
 def run_chain(kernel, num_results, current_state, num_burnin_steps=0,
               num_steps_between_results=0, seed=None, first_step=0, step_size=None,
-              da_state=None):
+              da_state=None, free_running_draws=False):
   """Device-resident ``sample_chain`` for the engine's NUTS / HMC kernels
   (optionally inside DualAveragingStepSizeAdaptation): the whole loop, the
   adaptation and the trace run in C++ on the device (gbm_*_sample_chain).
+
+  free_running_draws (NUTS): the results drawn at the final step size (past
+  the adaptation window, no thinning) come from the free-running loop
+  (gbm_nuts_set_free_running): per chain the same transitions, without
+  waiting for the batch's longest trajectory.
 
   Returns ChainRun(all_states [R, C, D], trace dict, final_state,
   final_step_size, final_da_state); pass the last three back (with
@@ -125,12 +130,18 @@ def run_chain(kernel, num_results, current_state, num_burnin_steps=0,
         P(tr['step_size'])), 'gbm_hmc_sample_chain')
   else:
     sampler._ensure(C)
-    _native.check(_native.lib().gbm_nuts_sample_chain(
-        sampler._handle, C, P(q), P(logp), P(grad), P(eps), per_chain,
-        _native.seed_words(seed), int(first_step), R, int(num_burnin_steps),
-        int(num_steps_between_results), *args, P(tr['state']), P(tr['target_log_prob']),
-        P(tr['log_accept_ratio']), P(tr['leapfrogs_taken']), P(tr['is_accepted']),
-        P(tr['has_divergence']), P(tr['step_size'])), 'gbm_nuts_sample_chain')
+    lib = _native.lib()
+    _native.check(lib.gbm_nuts_set_free_running(sampler._handle, int(bool(free_running_draws))),
+                  'gbm_nuts_set_free_running')
+    try:
+      _native.check(lib.gbm_nuts_sample_chain(
+          sampler._handle, C, P(q), P(logp), P(grad), P(eps), per_chain,
+          _native.seed_words(seed), int(first_step), R, int(num_burnin_steps),
+          int(num_steps_between_results), *args, P(tr['state']), P(tr['target_log_prob']),
+          P(tr['log_accept_ratio']), P(tr['leapfrogs_taken']), P(tr['is_accepted']),
+          P(tr['has_divergence']), P(tr['step_size'])), 'gbm_nuts_sample_chain')
+    finally:
+      lib.gbm_nuts_set_free_running(sampler._handle, 0)
   for k in ('is_accepted', 'has_divergence'):
     if k in tr:
       tr[k] = tr[k].bool()

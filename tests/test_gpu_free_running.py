@@ -103,3 +103,58 @@ def test_free_running_budget_keeps_completed_transitions(pg):
   for c in range(C):
     for t in range(done[c]):
       np.testing.assert_array_equal(cs[t, offs[c]:offs[c + 1]], fs[t, offs[c]:offs[c + 1]])
+
+
+def _mvn(pg, d=23, seed=8):
+  rng = np.random.default_rng(seed)
+  A = rng.standard_normal((d, d + 2)) / np.sqrt(d)
+  return pg.MultivariateNormalTriL(rng.normal(size=d), np.linalg.cholesky(A @ A.T))
+
+
+@pytest.mark.parametrize('burnin,adapt,results', [(6, 6, 14), (4, 11, 12), (12, 5, 9),
+                                                  (0, 0, 10)])
+def test_run_chain_free_running_draws_equal_lock_step(pg, burnin, adapt, results):
+  """sample_chain with the draws past the adaptation window free-running:
+  every result, the final state and the final dual-averaging state are
+  bit-equal to the lock-step loop on a multivariate normal (the window may
+  end before, at or after the burn-in)."""
+  t = _mvn(pg)
+  C = 40
+  q0 = torch.from_numpy((np.random.default_rng(1).normal(size=(C, 23)) * 0.3)
+                        .astype(np.float32)).cuda()
+  runs = []
+  for free in (False, True):
+    nuts = pg.mcmc.NoUTurnSampler(t, step_size=0.3, max_tree_depth=7)
+    k = pg.mcmc.DualAveragingStepSizeAdaptation(nuts, num_adaptation_steps=adapt,
+                                                target_accept_prob=0.75) if adapt else nuts
+    runs.append(pg.mcmc.run_chain(k, results, q0, num_burnin_steps=burnin, seed=(3, 9),
+                                  free_running_draws=free))
+  a, b = runs
+  assert torch.equal(a.all_states, b.all_states)
+  for key in a.trace:
+    assert torch.equal(a.trace[key], b.trace[key]), key
+  assert torch.equal(a.final_state, b.final_state)
+  assert torch.equal(a.final_step_size, b.final_step_size)
+  if adapt:
+    assert torch.equal(a.final_da_state, b.final_da_state)
+
+
+def test_run_chain_free_running_draws_logistic_regression(pg):
+  """Logistic regression: the kernels' row splits depend on how many chains
+  are evaluated together, so free-running and lock-step agree to rounding
+  (states 1e-5 relative on chains whose leapfrog counts agree)."""
+  X, y, _ = _problems.logreg_data(600, 8, seed=5, scale=0.5)
+  t = pg.LogisticRegression(X, y)
+  q0 = torch.from_numpy(_problems.init_state(64, 8, seed=4)).cuda()
+  runs = []
+  for free in (False, True):
+    k = pg.mcmc.DualAveragingStepSizeAdaptation(
+        pg.mcmc.NoUTurnSampler(t, step_size=0.1, max_tree_depth=7), num_adaptation_steps=8)
+    runs.append(pg.mcmc.run_chain(k, 6, q0, num_burnin_steps=8, seed=(2, 2),
+                                  free_running_draws=free))
+  a, b = runs
+  same = (a.trace['leapfrogs_taken'] == b.trace['leapfrogs_taken']).all(0).cpu().numpy()
+  assert same.mean() >= 0.9
+  np.testing.assert_allclose(b.all_states.cpu().numpy()[:, same], a.all_states.cpu().numpy()[:, same],
+                             rtol=1e-5, atol=1e-5)
+  np.testing.assert_allclose(b.final_step_size.cpu().numpy(), a.final_step_size.cpu().numpy())

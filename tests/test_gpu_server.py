@@ -1,5 +1,6 @@
-"""The job server (gbm_server_*): results equal the single-sampler path,
-are identical alone and in a concurrent mix, and admission respects the
+"""The job server (gbm_server_*): results equal the single-sampler path
+(run_chain with free-running draws, as the server runs its jobs), are
+identical alone and in a concurrent mix, and admission respects the
 device-memory budget."""
 import numpy as np
 import pytest
@@ -38,7 +39,7 @@ def test_server_job_equals_run_chain(pg):
       pg.mcmc.NoUTurnSampler(t, step_size=0.1, max_tree_depth=8), num_adaptation_steps=10,
       target_accept_prob=0.8)
   run = pg.mcmc.run_chain(k, 12, torch.from_numpy(_problems.init_state(32, 20, seed=3)).cuda(),
-                          num_burnin_steps=5, seed=(3, 1))
+                          num_burnin_steps=5, seed=(3, 1), free_running_draws=True)
   assert torch.equal(job.states, run.all_states)
   assert torch.equal(job.leapfrogs_taken, run.trace['leapfrogs_taken'])
   srv.close()
@@ -116,7 +117,7 @@ def test_server_job_beyond_the_fused_kernels_feature_limits(pg, d, precision):
       pg.mcmc.NoUTurnSampler(t, step_size=0.1, max_tree_depth=8), num_adaptation_steps=10,
       target_accept_prob=0.8)
   run = pg.mcmc.run_chain(k, 4, torch.from_numpy(_problems.init_state(24, d, seed=7)).cuda(),
-                          num_burnin_steps=5, seed=(7, 1))
+                          num_burnin_steps=5, seed=(7, 1), free_running_draws=True)
   assert torch.equal(job.states, run.all_states)
   assert torch.equal(job.leapfrogs_taken, run.trace['leapfrogs_taken'])
   srv.close()
