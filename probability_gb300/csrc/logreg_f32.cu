@@ -392,9 +392,10 @@ class LogregF32 final : public Target {
     const int lim = grid_ * kF32CT;
     for (int base = 0; base < cap; base += lim) {
       const float* qc = q + (size_t)base * ldq;
+      const int g = work_grid(grid_, std::min(lim, cap - base), kF32CT, N_, kMinSplitRows);
 #define GBM_F32_LAUNCH(KD_)                                                                \
-  logreg_f32_kernel<KD_><<<grid_, kF32Threads, F32Layout<KD_>::kBytes, s>>>(                \
-      x2_.as<float>(), ym_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart, gpart, \
+  logreg_f32_kernel<KD_><<<g, kF32Threads, F32Layout<KD_>::kBytes, s>>>(                    \
+      x2_.as<float>(), ym_.as<float>(), N, D, qc, ldq, n_dev, base, lim, g, lpart, gpart,     \
       err_dev_)
       switch (kd_) {
         case 1: GBM_F32_LAUNCH(1); break;
@@ -408,7 +409,7 @@ class LogregF32 final : public Target {
 #undef GBM_F32_LAUNCH
       GBM_CUDA(cudaGetLastError());
       launch_split_reduce(lpart, gpart, qc, ldq, n_dev, base, lim, std::min(lim, cap - base),
-                          kF32CT, kF32RT, grid_, N, D, inv_var_, log_norm_, lin_.as<double>(),
+                          kF32CT, kF32RT, g, N, D, inv_var_, log_norm_, lin_.as<double>(),
                           logp + base, grad + (size_t)base * ldg, ldg, s);
     }
   }

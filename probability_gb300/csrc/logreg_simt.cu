@@ -237,23 +237,24 @@ class LogregSimt final : public Target {
     const int lim = grid_ * kCT;
     for (int base = 0; base < cap; base += lim) {
       const float* qc = q + (size_t)base * ldq;
+      const int g = work_grid(grid_, std::min(lim, cap - base), kCT, N_, kMinSplitRows);
       switch (kd_) {
-        case 2: logreg_partial_kernel<2><<<grid_, kThreads, smem_, s>>>(
-            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart,
+        case 2: logreg_partial_kernel<2><<<g, kThreads, smem_, s>>>(
+            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, g, lpart,
             gpart); break;
-        case 4: logreg_partial_kernel<4><<<grid_, kThreads, smem_, s>>>(
-            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart,
+        case 4: logreg_partial_kernel<4><<<g, kThreads, smem_, s>>>(
+            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, g, lpart,
             gpart); break;
-        case 8: logreg_partial_kernel<8><<<grid_, kThreads, smem_, s>>>(
-            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart,
+        case 8: logreg_partial_kernel<8><<<g, kThreads, smem_, s>>>(
+            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, g, lpart,
             gpart); break;
-        default: logreg_partial_kernel<16><<<grid_, kThreads, smem_, s>>>(
-            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart,
+        default: logreg_partial_kernel<16><<<g, kThreads, smem_, s>>>(
+            x_.as<float>(), ldx_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, g, lpart,
             gpart); break;
       }
       GBM_CUDA(cudaGetLastError());
       launch_split_reduce(lpart, gpart, qc, ldq, n_dev, base, lim, std::min(lim, cap - base),
-                          kCT, kNT, grid_, N, D, inv_var_, log_norm_, nullptr, logp + base,
+                          kCT, kNT, g, N, D, inv_var_, log_norm_, nullptr, logp + base,
                           grad + (size_t)base * ldg, ldg, s);
     }
   }

@@ -897,7 +897,12 @@ struct PairLayout {
 };
 
 struct PairBars {
-  uint64_t x_full[2], x_empty[2], z_full[2], z_empty[2];
+  // X stages fill and drain in two halves of 32 KB (features 0-127 and
+  // 128-255 of the CTA's 256): the G MMAs of the first 128 features free the
+  // first half while those of the second still run, so the refill overlaps
+  // the tensor pipe instead of stalling the next tile's Z MMAs.
+  uint64_t x_full[2][2], x_empty[2][2];   // [stage][half]
+  uint64_t z_full[2], z_empty[2];
   uint64_t zx_full;   // peer's partial for my rows has arrived (8 remote arrivals)
   uint64_t zx_free;   // peer has read what I sent last (8 remote arrivals)
   uint64_t r_full;    // R tile complete (8 local + 8 remote arrivals)
@@ -960,8 +965,10 @@ logreg_tc_pair_kernel(const __grid_constant__ CUtensorMap xmap, const float* __r
   float lp_pub = 0.f;   // compute warps, lane j < 16: log-likelihood partial of chain 16 sub + j
   if (tid == 0) {
     for (int i = 0; i < 2; ++i) {
-      tc::mbar_init(&bars->x_full[i], 1);
-      tc::mbar_init(&bars->x_empty[i], 1);
+      for (int h = 0; h < 2; ++h) {
+        tc::mbar_init(&bars->x_full[i][h], 1);
+        tc::mbar_init(&bars->x_empty[i][h], 1);
+      }
       tc::mbar_init(&bars->z_full[i], 1);
       tc::mbar_init(&bars->z_empty[i], kPairEpi);
     }
@@ -1011,22 +1018,31 @@ logreg_tc_pair_kernel(const __grid_constant__ CUtensorMap xmap, const float* __r
   if (warp == 0) {
     // ---------------- TMA producer: X[rows, F_p] ----------------
     if (lane == 0) {
-      int it = 0;
-      for (; it < T; ++it) {
+      // Half-stage fills in order: fill f is (tile f / 2, half f % 2).
+      int nfill = 0;
+      bool stop = false;
+      for (int it = 0; it < T && !stop; ++it) {
         const int s = it & 1;
-        if (!wait_or_abort(&bars->x_empty[s], ((uint32_t)(it >> 1) & 1) ^ 1, abort_flag)) {
-          tc::record_error(err, kTcTimeoutTma);
-          abort_both();
-          break;
-        }
-        tc::mbar_arrive_expect_tx(&bars->x_full[s], L::kXStage);
+        for (int h = 0; h < 2; ++h) {
+          if (!wait_or_abort(&bars->x_empty[s][h], ((uint32_t)(it >> 1) & 1) ^ 1, abort_flag)) {
+            tc::record_error(err, kTcTimeoutTma);
+            abort_both();
+            stop = true;
+            break;
+          }
+          tc::mbar_arrive_expect_tx(&bars->x_full[s][h], L::kXStage / 2);
 #pragma unroll
-        for (int kb = 0; kb < kPairKB; ++kb)
-          tc::tma_load_2d(Xs + s * L::kXStage + kb * 16384, &xmap, f0 + kb * 64,
-                          (rt_begin + it) * kRows, &bars->x_full[s]);
+          for (int kb = 2 * h; kb < 2 * h + 2; ++kb)
+            tc::tma_load_2d(Xs + s * L::kXStage + kb * 16384, &xmap, f0 + kb * 64,
+                            (rt_begin + it) * kRows, &bars->x_full[s][h]);
+          ++nfill;
+        }
       }
-      for (int j = (it > 2 ? it - 2 : 0); j < it; ++j)
-        tc::mbar_wait(&bars->x_full[j & 1], (uint32_t)((j >> 1) & 1), kWaitLimitNs);
+      // Let the last fills land before the CTA can exit (each wait bounded).
+      for (int f = (nfill > 4 ? nfill - 4 : 0); f < nfill; ++f) {
+        const int j = f >> 1, h = f & 1;
+        tc::mbar_wait(&bars->x_full[j & 1][h], (uint32_t)((j >> 1) & 1), kWaitLimitNs);
+      }
     }
     __syncwarp();
   } else if (warp == 1) {
@@ -1043,21 +1059,27 @@ logreg_tc_pair_kernel(const __grid_constant__ CUtensorMap xmap, const float* __r
       auto gemm1 = [&](int it) -> bool {
         const int s = it & 1, b = it & 1;
         const uint32_t use = (uint32_t)(it >> 1) & 1;
-        if (!wait_or_abort(&bars->x_full[s], use, abort_flag)) return false;
         if (!wait_or_abort(&bars->z_empty[b], use ^ 1, abort_flag)) return false;
-        tc::tc_fence_after();
         const uint32_t tz = tmem + b * CT;
         const uint32_t xa = xs_a + s * L::kXStage;
+        // Half h holds K-steps 8h .. 8h + 7; a half without data (fD <= 128)
+        // is neither waited for nor read.
+        for (int h = 0; h < 2 && 8 * h < ksteps; ++h) {
+          if (!wait_or_abort(&bars->x_full[s][h], use, abort_flag)) return false;
+          tc::tc_fence_after();
 #pragma unroll
-        for (int kb = 0; kb < kPairKB; ++kb) {
+          for (int kb = 2 * h; kb < 2 * h + 2; ++kb) {
 #pragma unroll
-          for (int k = 0; k < 4; ++k) {
-            if (kb * 4 + k >= ksteps) break;
-            const uint64_t a = tc::smem_desc_sw128(xa + kb * 16384 + k * 32, 16, 1024);
-            const uint64_t bh = tc::smem_desc_sw128(bhi_a + kb * (CT * 128) + k * 32, 16, 1024);
-            const uint64_t bl = tc::smem_desc_sw128(blo_a + kb * (CT * 128) + k * 32, 16, 1024);
-            tc::mma_bf16(tz, a, bh, idesc1, (kb | k) ? 1u : 0u);
-            tc::mma_bf16(tz, a, bl, idesc1, 1u);
+            for (int k = 0; k < 4; ++k) {
+              if (kb * 4 + k >= ksteps) break;
+              const uint64_t a = tc::smem_desc_sw128(xa + kb * 16384 + k * 32, 16, 1024);
+              const uint64_t bh =
+                  tc::smem_desc_sw128(bhi_a + kb * (CT * 128) + k * 32, 16, 1024);
+              const uint64_t bl =
+                  tc::smem_desc_sw128(blo_a + kb * (CT * 128) + k * 32, 16, 1024);
+              tc::mma_bf16(tz, a, bh, idesc1, (kb | k) ? 1u : 0u);
+              tc::mma_bf16(tz, a, bl, idesc1, 1u);
+            }
           }
         }
         tc::mma_commit(&bars->z_full[b]);
@@ -1075,6 +1097,8 @@ logreg_tc_pair_kernel(const __grid_constant__ CUtensorMap xmap, const float* __r
         }
         tc::tc_fence_after();
         const uint32_t xa = xs_a + (it & 1) * L::kXStage;
+        // M-tile mt reads half mt of the stage; each half is released as soon
+        // as the MMAs that read it (and every earlier one) complete.
         for (int mt = 0; mt < mtiles; ++mt) {
 #pragma unroll
           for (int ks = 0; ks < kRows / 16; ++ks) {
@@ -1082,8 +1106,9 @@ logreg_tc_pair_kernel(const __grid_constant__ CUtensorMap xmap, const float* __r
             const uint64_t bd = tc::smem_desc_sw128(rs_a + ks * 2048, 16384, 1024);
             tc::mma_bf16(tg + mt * CT, a, bd, idesc2, (it > 0 || ks > 0) ? 1u : 0u);
           }
+          tc::mma_commit(&bars->x_empty[it & 1][mt]);
         }
-        tc::mma_commit(&bars->x_empty[it & 1]);
+        if (mtiles == 1) tc::mma_commit(&bars->x_empty[it & 1][1]);
         tc::mma_commit_multicast(&bars->r_free, (uint16_t)0x3);
       }
       if (ok) {
@@ -1443,26 +1468,28 @@ class LogregTc final : public Target {
     const int lim = grid_ * ct_;
     for (int base = 0; base < cap; base += lim) {
       const float* qc = q + (size_t)base * ldq;
+      // Work items of this launch (CTAs, or CTA pairs for the pair kernel).
+      const int g = work_grid(grid_, std::min(lim, cap - base), ct_, N_, kMinSplitRows);
 #define GBM_TC_LAUNCH(KB_, CT_, EPI_, XLO_)                                               \
-  logreg_tc_kernel<KB_, CT_, EPI_, XLO_><<<grid_, tc_threads(EPI_), smem_, s>>>(          \
-      xmap_, xlomap_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart, gpart, \
+  logreg_tc_kernel<KB_, CT_, EPI_, XLO_><<<g, tc_threads(EPI_), smem_, s>>>(              \
+      xmap_, xlomap_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, g, lpart, gpart,     \
       err_dev_)
 #define GBM_TCT_LAUNCH(XLO_)                                                              \
-  logreg_tct_kernel<XLO_><<<grid_, tc_threads(kTctEpi), smem_, s>>>(                       \
-      xmap_, xlomap_, ym_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart, gpart, \
+  logreg_tct_kernel<XLO_><<<g, tc_threads(kTctEpi), smem_, s>>>(                           \
+      xmap_, xlomap_, ym_.as<float>(), N, D, qc, ldq, n_dev, base, lim, g, lpart, gpart,     \
       err_dev_)
       if (kb_ == 2 && xlo_) GBM_TCT_LAUNCH(true);
       else if (kb_ == 2) GBM_TCT_LAUNCH(false);
       else if (kb_ == 4) GBM_TC_LAUNCH(4, 64, 8, false);
       else
-        logreg_tc_pair_kernel<<<2 * grid_, tc_threads(kPairEpi), smem_, s>>>(
-            xmap_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, grid_, lpart, gpart,
+        logreg_tc_pair_kernel<<<2 * g, tc_threads(kPairEpi), smem_, s>>>(
+            xmap_, y_.as<float>(), N, D, qc, ldq, n_dev, base, lim, g, lpart, gpart,
             err_dev_);
 #undef GBM_TC_LAUNCH
 #undef GBM_TCT_LAUNCH
       GBM_CUDA(cudaGetLastError());
       launch_split_reduce(lpart, gpart, qc, ldq, n_dev, base, lim, std::min(lim, cap - base),
-                          ct_, kRows, grid_, N, D, inv_var_, log_norm_, lin_.as<double>(),
+                          ct_, kRows, g, N, D, inv_var_, log_norm_, lin_.as<double>(),
                           logp + base, grad + (size_t)base * ldg, ldg, s);
     }
   }

@@ -112,8 +112,69 @@ void set_count(int* count, int n, cudaStream_t s) {
   GBM_CUDA(cudaGetLastError());
 }
 
+// Large batches: per-block counts, then an order-preserving scatter (each
+// block adds the counts of the blocks before it), so the list stays sorted.
+constexpr int kActBlock = 1024;
+
+__global__ void active_block_count_kernel(const uint8_t* __restrict__ flags, uint8_t bit, int C,
+                                          int* __restrict__ blk) {
+  const int c = blockIdx.x * kActBlock + threadIdx.x;
+  const int n = __syncthreads_count(c < C && (flags[c] & bit));
+  if (threadIdx.x == 0) blk[blockIdx.x] = n;
+}
+
+__global__ void active_block_scatter_kernel(const uint8_t* __restrict__ flags, uint8_t bit, int C,
+                                            const int* __restrict__ blk, int* __restrict__ idx,
+                                            int* __restrict__ count) {
+  __shared__ int warp_tot[32];
+  __shared__ int base_s;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5;
+  const int nw = kActBlock >> 5;
+  int part = 0;
+  for (int b = tid; b < (int)blockIdx.x; b += kActBlock) part += blk[b];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) part += __shfl_xor_sync(0xffffffffu, part, o);
+  if (lane == 0) warp_tot[w] = part;
+  __syncthreads();
+  if (tid == 0) {
+    int sum = 0;
+    for (int i = 0; i < nw; ++i) sum += warp_tot[i];
+    base_s = sum;
+  }
+  __syncthreads();
+  const int base = base_s;
+  const int c = blockIdx.x * kActBlock + tid;
+  const bool on = c < C && (flags[c] & bit);
+  const unsigned m = __ballot_sync(0xffffffffu, on);
+  __syncthreads();   // everyone has read warp_tot's block sums
+  if (lane == 0) warp_tot[w] = __popc(m);
+  __syncthreads();
+  if (w == 0) {
+    const int v = lane < nw ? warp_tot[lane] : 0;
+    int incl = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int t = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += t;
+    }
+    if (lane < nw) warp_tot[lane] = incl - v;   // exclusive
+  }
+  __syncthreads();
+  if (on) idx[base + warp_tot[w] + __popc(m & ((1u << lane) - 1u))] = c;
+  if (tid == 0 && blockIdx.x == gridDim.x - 1) *count = base + blk[blockIdx.x];
+}
+
+static int active_launches(int C) { return C <= 2 * kActBlock ? 1 : 2; }
+
 static void build_active(const NutsDev& d, uint8_t bit, cudaStream_t s) {
-  build_active_kernel<<<1, 1024, 0, s>>>(d.flags, bit, d.C, d.act_idx, d.act_count);
+  if (d.C <= 2 * kActBlock) {
+    build_active_kernel<<<1, 1024, 0, s>>>(d.flags, bit, d.C, d.act_idx, d.act_count);
+  } else {
+    const int nb = (d.C + kActBlock - 1) / kActBlock;
+    active_block_count_kernel<<<nb, kActBlock, 0, s>>>(d.flags, bit, d.C, d.act_blk);
+    active_block_scatter_kernel<<<nb, kActBlock, 0, s>>>(d.flags, bit, d.C, d.act_blk,
+                                                         d.act_idx, d.act_count);
+  }
   GBM_CUDA(cudaGetLastError());
 }
 
@@ -788,7 +849,8 @@ void nuts_setup(gbm_nuts* k) {
   size_t off_f = take(sizeof(float) * vec * n_float_vecs);
   size_t off_slots = take(sizeof(float) * vec * slots * 2);
   size_t off_d = take(sizeof(double) * C * 12);
-  size_t off_i = take(sizeof(int) * C * 4 + 64);
+  const size_t nblk = (size_t)((C + 1023) / 1024);
+  size_t off_i = take(sizeof(int) * (C * 4 + 16 + nblk));
   size_t off_b = take(C);
   size_t off_e = take(sizeof(float) * C);
   k->mem.reserve(bytes);
@@ -811,7 +873,7 @@ void nuts_setup(gbm_nuts* k) {
   w.e0 = dv + 8 * C; w.eds = dv + 9 * C; w.sub_eds = dv + 10 * C; w.lw = dv + 11 * C;
   int* iv = reinterpret_cast<int*>(base + off_i);
   w.lf = iv; w.sub_lf = iv + C; w.tree_depth = iv + 2 * C; w.act_idx = iv + 3 * C;
-  w.act_count = iv + 4 * C; w.any_cont = iv + 4 * C + 1;
+  w.act_count = iv + 4 * C; w.any_cont = iv + 4 * C + 1; w.act_blk = iv + 4 * C + 16;
   w.flags = reinterpret_cast<uint8_t*>(base + off_b);
   w.eps = reinterpret_cast<float*>(base + off_e);
   GBM_CUDA(cudaMemsetAsync(base, 0, bytes, k->ctx->stream));
@@ -839,11 +901,6 @@ void nuts_release_graphs(gbm_nuts* k) {
 
 static void nuts_eval(gbm_nuts* k, cudaStream_t s, bool capturing = false) {
   const NutsDev& w = k->dev;
-  if (w.ragged) {
-    k->target->impl->eval_active(w.qw, w.act_idx, w.act_count, w.lw, w.gw, k->target_ws.ptr, s);
-    if (!capturing) k->prof_launches += k->target->impl->launches_per_eval(w.C);
-    return;
-  }
   if (k->profiling && !capturing) {
     if (k->prof_used + 2 > k->prof_events.size()) {
       cudaEvent_t a, b;
@@ -854,7 +911,10 @@ static void nuts_eval(gbm_nuts* k, cudaStream_t s, bool capturing = false) {
     }
     GBM_CUDA(cudaEventRecord(k->prof_events[k->prof_used], s));
   }
-  k->target->impl->eval(w.qw, w.D, w.act_count, w.C, w.lw, w.gw, w.D, k->target_ws.ptr, s);
+  if (w.ragged)
+    k->target->impl->eval_active(w.qw, w.act_idx, w.act_count, w.lw, w.gw, k->target_ws.ptr, s);
+  else
+    k->target->impl->eval(w.qw, w.D, w.act_count, w.C, w.lw, w.gw, w.D, k->target_ws.ptr, s);
   if (!capturing) k->prof_launches += k->target->impl->launches_per_eval(w.C);
   if (k->profiling && !capturing) {
     GBM_CUDA(cudaEventRecord(k->prof_events[k->prof_used + 1], s));
@@ -903,7 +963,8 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
         k->max_energy_diff);
     GBM_CUDA(cudaGetLastError());
     build_active(w, kSubCont, ls);
-    if (!capturing) k->prof_launches += 3 + (k->unrolled_leapfrog_steps - 1);
+    if (!capturing)
+      k->prof_launches += 2 + active_launches(w.C) + (k->unrolled_leapfrog_steps - 1);
   };
   // Profiled steps time every gradient evaluation with events: leaf by leaf.
   const bool graphs = k->use_graphs && !k->profiling;
@@ -955,7 +1016,8 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
         }
         GBM_CUDA(cudaGraphLaunch(it->second, s));
         ++k->graph_launches;
-        k->prof_launches += (int64_t)nl * (3 + k->unrolled_leapfrog_steps * (
+        k->prof_launches += (int64_t)nl * (2 + active_launches(w.C) +
+                                           k->unrolled_leapfrog_steps * (
             k->target->impl->launches_per_eval(chains) + 1) - 1);
         k->last_leaf_iterations += nl;
         leaf += nl - 1;
@@ -966,7 +1028,7 @@ void nuts_one_step(gbm_nuts* k, int64_t chains, const float* q, const double* l,
     }
     nuts_depth_end_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, key, depth);
     GBM_CUDA(cudaGetLastError());
-    k->prof_launches += 4;
+    k->prof_launches += 3 + active_launches(w.C);
   }
   nuts_finalize_kernel<<<wb, 32 * kWarpsPerBlock, 0, s>>>(w, out, k->unrolled_leapfrog_steps);
   GBM_CUDA(cudaGetLastError());
@@ -1027,7 +1089,7 @@ int64_t nuts_run_free(gbm_nuts* k, int64_t chains, const float* q, const double*
     nuts_eval(k, ls, capturing);
     nuts_free_post_kernel<<<wb, 32 * kWarpsPerBlock, 0, ls>>>(w, f);
     GBM_CUDA(cudaGetLastError());
-    if (!capturing) k->prof_launches += 3;
+    if (!capturing) k->prof_launches += 2 + active_launches(C);
   };
   // Batches of `batch` iterations, replayed as one CUDA graph (captured for
   // this call: its pointers are the call's); the host polls the running count
@@ -1052,7 +1114,8 @@ int64_t nuts_run_free(gbm_nuts* k, int64_t chains, const float* q, const double*
       const int64_t n = std::min<int64_t>(batch, max_leaf_iterations - iters);
       if (exec && n == batch) {
         GBM_CUDA(cudaGraphLaunch(exec, s));
-        k->prof_launches += (int64_t)batch * (3 + k->target->impl->launches_per_eval(C));
+        k->prof_launches +=
+            (int64_t)batch * (2 + active_launches(C) + k->target->impl->launches_per_eval(C));
       } else {
         for (int64_t i = 0; i < n; ++i) iteration(s, false);
       }

@@ -85,6 +85,7 @@ struct NutsDev {
   float* eps;               // |step size| per chain
   int* act_idx;             // [C]
   int* act_count;           // [1]
+  int* act_blk;             // [ceil(C / 1024)] per-block counts of the compaction
   int* any_cont;            // [1]
 };
 

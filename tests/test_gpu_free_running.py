@@ -158,3 +158,24 @@ def test_run_chain_free_running_draws_logistic_regression(pg):
   np.testing.assert_allclose(b.all_states.cpu().numpy()[:, same], a.all_states.cpu().numpy()[:, same],
                              rtol=1e-5, atol=1e-5)
   np.testing.assert_allclose(b.final_step_size.cpu().numpy(), a.final_step_size.cpu().numpy())
+
+
+def test_large_batches_compact_the_same_chains(pg):
+  """Above 2048 chains the active list is built by the multi-block
+  compaction.  Draws are addressed by chain index, so on a multivariate
+  normal chains 0..999 of a 3000-chain batch must equal a 1000-chain batch
+  bit for bit, in lock-step and free-running."""
+  t = _mvn(pg, d=9, seed=3)
+  rng = np.random.default_rng(6)
+  q_big = torch.from_numpy((rng.normal(size=(3000, 9)) * 0.4).astype(np.float32)).cuda()
+  q_small = q_big[:1000].clone()
+  out = []
+  for q in (q_big, q_small):
+    k = pg.mcmc.NoUTurnSampler(t, step_size=0.25, max_tree_depth=8)
+    kr = k.bootstrap_results(q)
+    q1, kr1 = k.one_step(q, kr, seed=(4, 4))
+    run = k.run_free(q, kr, 3, (4, 5))
+    out.append((q1[:1000], kr1.leapfrogs_taken[:1000], run.all_states[:, :1000],
+                run.trace['leapfrogs_taken'][:, :1000]))
+  for a, b in zip(*out):
+    assert torch.equal(a, b)

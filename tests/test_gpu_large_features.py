@@ -29,7 +29,8 @@ def pg():
   return pg
 
 
-@pytest.mark.parametrize('n,d,c', [(3000, 300, 70), (1500, 700, 129), (777, 257, 3)])
+@pytest.mark.parametrize('n,d,c', [(3000, 300, 70), (1500, 700, 129), (777, 257, 3),
+                                   (9000, 400, 50)])
 def test_fp32_above_256_features(pg, n, d, c):
   X, y, _ = _problems.logreg_data(n, d, seed=d, scale=d ** -0.5)
   t = pg.LogisticRegression(X, y, precision='fp32')
@@ -42,7 +43,8 @@ def test_fp32_above_256_features(pg, n, d, c):
 
 
 @pytest.mark.parametrize('n,d,c,bf16', [(3000, 600, 64, True), (2000, 1000, 200, True),
-                                        (1000, 513, 1, True), (2500, 800, 33, False)])
+                                        (1000, 513, 1, True), (2500, 800, 33, False),
+                                        (9000, 600, 33, True), (8192, 700, 40, False)])
 def test_mixed_above_512_features(pg, n, d, c, bf16):
   X, y, _ = _problems.logreg_data(n, d, seed=d + 1, scale=d ** -0.5)
   if bf16:
