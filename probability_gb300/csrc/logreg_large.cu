@@ -120,12 +120,12 @@ __global__ void large_split_states(const float* __restrict__ q, int ldq, int n, 
 // (1/(1 + e^-|z|) - 1/2) (hi, and lo in the mixed form).
 template <class TO>
 __global__ void __launch_bounds__(256)
-large_epilogue(const float* __restrict__ Z, const float* __restrict__ ym, int64_t N, int n,
-               TO* __restrict__ Rhi, TO* __restrict__ Rlo, double* __restrict__ part) {
+large_epilogue(const float* __restrict__ Z, const float* __restrict__ ym, int64_t N, int64_t ldz,
+               int n, TO* __restrict__ Rhi, TO* __restrict__ Rlo, double* __restrict__ part) {
   __shared__ double red[8];
   const int64_t r0 = (int64_t)blockIdx.x * kRowBlock;
   for (int c = blockIdx.y; c < n; c += gridDim.y) {   // grid.y is capped at 65535
-    const float* z = Z + (size_t)c * N;
+    const float* z = Z + (size_t)c * ldz;
     double acc = 0.0;
     for (int64_t r = r0 + threadIdx.x; r < r0 + kRowBlock && r < N; r += blockDim.x) {
       const float zv = z[r];
@@ -136,8 +136,8 @@ large_epilogue(const float* __restrict__ Z, const float* __restrict__ ym, int64_
       const float w = tc::rcp_approx(u) - 0.5f;
       const float rv = zv >= 0.f ? ym[r] - w : ym[r] + w;
       const TO h = from_float<TO>(rv);
-      Rhi[(size_t)c * N + r] = h;
-      if (Rlo) Rlo[(size_t)c * N + r] = from_float<TO>(rv - (float)h);
+      Rhi[(size_t)c * ldz + r] = h;
+      if (Rlo) Rlo[(size_t)c * ldz + r] = from_float<TO>(rv - (float)h);
     }
     acc = warp_sum(acc);
     __syncthreads();                                   // red[] of the previous chain is read
@@ -179,6 +179,7 @@ class LogregLarge final : public Target {
       : N_(n), D_(d), mixed_(mixed), device_(ctx->device) {
     dim = d;
     ld_ = (int)((d + 7) / 8 * 8);
+    ldz_ = (N_ + 7) / 8 * 8;
     xlo_ = mixed && x_dtype == 0;
     const size_t el = mixed ? 2 : 4;
     xh_.reserve(el * (size_t)N_ * ld_);
@@ -225,8 +226,8 @@ class LogregLarge final : public Target {
   size_t workspace_bytes(int64_t cap) const override {
     const size_t el = mixed_ ? 2 : 4;
     const size_t nblk = (size_t)((N_ + kRowBlock - 1) / kRowBlock);
-    return align256(el * cap * ld_) * 2 + align256(4 * (size_t)N_ * cap) +
-           align256(el * (size_t)N_ * cap) * 2 + align256(4 * (size_t)cap * ld_) +
+    return align256(el * cap * ld_) * 2 + align256(4 * (size_t)ldz_ * cap) +
+           align256(el * (size_t)ldz_ * cap) * 2 + align256(4 * (size_t)cap * ld_) +
            align256(8 * nblk * cap) + kCublasWs;
   }
 
@@ -237,9 +238,9 @@ class LogregLarge final : public Target {
     unsigned char* p = static_cast<unsigned char*>(ws);
     void* bhi = p;                 p += align256(el * cap * ld_);
     void* blo = p;                 p += align256(el * cap * ld_);
-    float* Z = reinterpret_cast<float*>(p);    p += align256(4 * (size_t)N_ * cap);
-    void* rhi = p;                 p += align256(el * (size_t)N_ * cap);
-    void* rlo = p;                 p += align256(el * (size_t)N_ * cap);
+    float* Z = reinterpret_cast<float*>(p);    p += align256(4 * (size_t)ldz_ * cap);
+    void* rhi = p;                 p += align256(el * (size_t)ldz_ * cap);
+    void* rlo = p;                 p += align256(el * (size_t)ldz_ * cap);
     float* G = reinterpret_cast<float*>(p);    p += align256(4 * (size_t)cap * ld_);
     double* part = reinterpret_cast<double*>(p); p += align256(8 * (size_t)nblk * cap);
     void* cws = p;
@@ -257,10 +258,14 @@ class LogregLarge final : public Target {
     GBM_CUDA(cudaGetLastError());
     const cudaDataType_t dt = mixed_ ? CUDA_R_16BF : CUDA_R_32F;
     const float one = 1.f, zero = 0.f;
-    // Z = X_hi B_hi^T (+ X_hi B_lo^T + X_lo B_hi^T): column-major (N x n).
+    // Z = X_hi B_hi^T (+ X_hi B_lo^T + X_lo B_hi^T): column-major (N x n),
+    // leading dimension ldz_ (N rounded up to 8 rows) so every column starts
+    // 16-byte aligned; K runs over the ld_ zero-padded features (a multiple
+    // of 8; the padding of X and of B is zero, so the sums are unchanged).
+    const int Kp = ld_, ldz = (int)ldz_;
     auto gemm_z = [&](const void* xa, const void* bb, const float* beta) {
-      GBM_CUBLAS(cublasGemmEx(h, CUBLAS_OP_T, CUBLAS_OP_N, N, n, D, &one, xa, dt, ld_, bb, dt,
-                              ld_, beta, Z, CUDA_R_32F, N, CUBLAS_COMPUTE_32F,
+      GBM_CUBLAS(cublasGemmEx(h, CUBLAS_OP_T, CUBLAS_OP_N, N, n, Kp, &one, xa, dt, ld_, bb, dt,
+                              ld_, beta, Z, CUDA_R_32F, ldz, CUBLAS_COMPUTE_32F,
                               CUBLAS_GEMM_DEFAULT));
     };
     gemm_z(xh_.ptr, bhi, &zero);
@@ -271,16 +276,17 @@ class LogregLarge final : public Target {
     const dim3 eg((unsigned)nblk, (unsigned)std::min(n, 65535));
     if (mixed_)
       large_epilogue<__nv_bfloat16><<<eg, 256, 0, s>>>(
-          Z, ym_.as<float>(), N_, n, static_cast<__nv_bfloat16*>(rhi),
+          Z, ym_.as<float>(), N_, ldz_, n, static_cast<__nv_bfloat16*>(rhi),
           static_cast<__nv_bfloat16*>(rlo), part);
     else
-      large_epilogue<float><<<eg, 256, 0, s>>>(Z, ym_.as<float>(), N_, n,
+      large_epilogue<float><<<eg, 256, 0, s>>>(Z, ym_.as<float>(), N_, ldz_, n,
                                                static_cast<float*>(rhi), nullptr, part);
     GBM_CUDA(cudaGetLastError());
-    // G^T = X_hi^T R_hi (+ X_hi^T R_lo + X_lo^T R_hi): column-major (ld x n).
+    // G^T = X_hi^T R_hi (+ X_hi^T R_lo + X_lo^T R_hi): column-major (ld x n)
+    // over all ld_ padded features (rows >= D come out zero and are not read).
     auto gemm_g = [&](const void* xa, const void* rr, const float* beta) {
-      GBM_CUBLAS(cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, D, n, N, &one, xa, dt, ld_, rr, dt,
-                              N, beta, G, CUDA_R_32F, ld_, CUBLAS_COMPUTE_32F,
+      GBM_CUBLAS(cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, Kp, n, N, &one, xa, dt, ld_, rr, dt,
+                              ldz, beta, G, CUDA_R_32F, ld_, CUBLAS_COMPUTE_32F,
                               CUBLAS_GEMM_DEFAULT));
     };
     gemm_g(xh_.ptr, rhi, &zero);
@@ -305,6 +311,7 @@ class LogregLarge final : public Target {
   int64_t N_, D_;
   bool mixed_, xlo_ = false;
   int device_ = 0, ld_ = 8;
+  int64_t ldz_ = 8;   // leading dimension of Z and R: N rounded up to 8 rows
   float inv_var_ = 1.f;
   double log_norm_ = 0.0;
   DeviceBuffer xh_, xl_, ym_, lin_;
