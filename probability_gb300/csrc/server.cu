@@ -185,17 +185,38 @@ void run_job(gbm_context* ctx, Job* job) {
   nuts_release_graphs(&k);
 }
 
+// Multiply-adds of one batched gradient evaluation of the job's chains.
+double leaf_work(const gbm_job_spec& s) {
+  const double C = (double)s.chains;
+  switch (s.family) {
+    case GBM_FAMILY_LOGISTIC_REGRESSION: return (double)s.rows * (double)s.features * C;
+    case GBM_FAMILY_MVN: return (double)s.dim * (double)s.dim * C;
+    default: return 10.0 * (double)s.groups * C;
+  }
+}
+
+// Jobs below this much work per leaf run on the worker's high-priority
+// stream: their kernels' blocks are scheduled ahead of the large jobs'
+// pending blocks whenever SMs free up, so a few large jobs do not multiply
+// the latency of every small one.
+constexpr double kSmallLeafWork = 2e9;
+
 void worker_main(gbm_server* srv) {
   cudaSetDevice(srv->device);
-  gbm_context ctx;
-  cudaStream_t stream = nullptr;
+  gbm_context ctx_hi, ctx_lo;
   try {
-    GBM_CUDA(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-    context_init(&ctx, srv->device, stream, true);
+    int least = 0, greatest = 0;
+    GBM_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    cudaStream_t s_hi = nullptr, s_lo = nullptr;
+    GBM_CUDA(cudaStreamCreateWithPriority(&s_hi, cudaStreamNonBlocking, greatest));
+    context_init(&ctx_hi, srv->device, s_hi, true);
+    GBM_CUDA(cudaStreamCreateWithPriority(&s_lo, cudaStreamNonBlocking, least));
+    context_init(&ctx_lo, srv->device, s_lo, true);
   } catch (...) {
+    context_free(&ctx_hi);
+    context_free(&ctx_lo);
     return;
   }
-  alloc_stream() = stream;
   while (true) {
     Job* job = nullptr;
     {
@@ -214,8 +235,10 @@ void worker_main(gbm_server* srv) {
     }
     int code = GBM_OK;
     std::string msg;
+    gbm_context* ctx = leaf_work(job->spec) < kSmallLeafWork ? &ctx_hi : &ctx_lo;
+    alloc_stream() = ctx->stream;
     try {
-      run_job(&ctx, job);
+      run_job(ctx, job);
     } catch (const CudaError& e) {
       code = e.err == cudaErrorMemoryAllocation ? GBM_ENOMEM : GBM_ECUDA;
       msg = std::string(e.what) + ": " + cudaGetErrorString(e.err);
@@ -226,7 +249,7 @@ void worker_main(gbm_server* srv) {
       code = GBM_ENOTSUP;
       msg = e.what();
     }
-    if (code != GBM_OK) cudaStreamSynchronize(stream);
+    if (code != GBM_OK) cudaStreamSynchronize(ctx->stream);
     {
       std::lock_guard<std::mutex> lock(srv->mu);
       srv->in_use -= job->bytes;
@@ -239,7 +262,8 @@ void worker_main(gbm_server* srv) {
     srv->work_cv.notify_all();
   }
   alloc_stream() = nullptr;
-  context_free(&ctx);
+  context_free(&ctx_hi);
+  context_free(&ctx_lo);
 }
 
 void fill_info(const Job* j, gbm_job_info* info) {
