@@ -14,7 +14,9 @@
 // states are split into BF16 hi + lo, R into BF16 hi + lo, and the products
 // X_hi B_hi^T + X_hi B_lo^T (+ X_lo B_hi^T) and X_hi^T R_hi + X_hi^T R_lo
 // (+ X_lo^T R_hi) are accumulated in FP32 -- the residual correction of the
-// fused tensor-core kernels.  FP32: both GEMMs in FP32 (no TF32).
+// fused tensor-core kernels.  The hi and lo splits sit side by side as 2n
+// columns, so each contraction is one GEMM (plus one for X_lo).  FP32: both
+// GEMMs in FP32 (no TF32).
 //
 // This target evaluates all `cap` states of a call (the GEMM shapes are host
 // values): a sampler's inactive rows are computed and ignored.  Every GEMM
@@ -36,6 +38,8 @@ namespace {
 
 constexpr size_t kCublasWs = 32u << 20;   // cuBLAS workspace inside the target workspace
 constexpr int kRowBlock = 2048;           // rows per epilogue block
+constexpr int kEpiThreads = 256;          // epilogue block size
+constexpr int kEpiRows = kRowBlock / kEpiThreads;
 constexpr float kNegLog2eL = -1.4426950408889634f;
 constexpr float kLn2L = 0.6931471805599453f;
 
@@ -62,18 +66,19 @@ template <> __device__ __forceinline__ __nv_bfloat16 from_float<__nv_bfloat16>(f
   return __float2bfloat16_rn(v);
 }
 
-// X [N][D] (float32 or BF16) -> hi [N][ld] (and lo for FP32 data in the
+// X [N][D] (float32 or BF16) -> hi [Np][ld] (and lo for FP32 data in the
 // mixed form), zero-padded features; ym = y - 1/2.
+// Rows N .. Np - 1 (the padding to a multiple of 8 rows) are zero.
 template <class TI, class TO>
 __global__ void large_pack_kernel(const TI* __restrict__ X, const float* __restrict__ y,
-                                  int64_t N, int D, int ld, TO* __restrict__ hi,
+                                  int64_t N, int64_t Np, int D, int ld, TO* __restrict__ hi,
                                   TO* __restrict__ lo, float* __restrict__ ym) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < N) ym[i] = y[i] - 0.5f;
-  if (i >= N * ld) return;
+  if (i < Np) ym[i] = i < N ? y[i] - 0.5f : 0.f;
+  if (i >= Np * ld) return;
   const int64_t r = i / ld;
   const int d = (int)(i - r * ld);
-  const float v = d < D ? (float)X[r * D + d] : 0.f;
+  const float v = (d < D && r < N) ? (float)X[r * D + d] : 0.f;
   const TO h = from_float<TO>(v);
   hi[i] = h;
   if (lo) lo[i] = from_float<TO>(v - (float)h);
@@ -119,29 +124,51 @@ __global__ void large_split_states(const float* __restrict__ q, int ldq, int n, 
 // of |z|/2 + ln(1 + e^-|z|) (float64 partial) and R = (y - 1/2) - sign(z)
 // (1/(1 + e^-|z|) - 1/2) (hi, and lo in the mixed form).
 template <class TO>
-__global__ void __launch_bounds__(256)
-large_epilogue(const float* __restrict__ Z, const float* __restrict__ ym, int64_t N, int64_t ldz,
-               int n, TO* __restrict__ Rhi, TO* __restrict__ Rlo, double* __restrict__ part) {
+__global__ void __launch_bounds__(kEpiThreads)
+large_epilogue(const float* __restrict__ Z, const float* __restrict__ Zlo,
+               const float* __restrict__ ym, int64_t N, int64_t ldz, int n,
+               TO* __restrict__ Rhi, TO* __restrict__ Rlo, double* __restrict__ part) {
   __shared__ double red[8];
   const int64_t r0 = (int64_t)blockIdx.x * kRowBlock;
   for (int c = blockIdx.y; c < n; c += gridDim.y) {   // grid.y is capped at 65535
     const float* z = Z + (size_t)c * ldz;
-    double acc = 0.0;
-    for (int64_t r = r0 + threadIdx.x; r < r0 + kRowBlock && r < N; r += blockDim.x) {
-      const float zv = z[r];
-      const float a = fabsf(zv);
+    const float* zl = Zlo ? Zlo + (size_t)c * ldz : nullptr;
+    // A thread's kEpiRows rows (stride blockDim): every load is issued before
+    // any use, so the block waits for memory once per chain, not per row.
+    float zv[kEpiRows], yv[kEpiRows];
+#pragma unroll
+    for (int k = 0; k < kEpiRows; ++k) {
+      const int64_t r = r0 + threadIdx.x + (int64_t)kEpiThreads * k;
+      zv[k] = 0.f;
+      yv[k] = 0.f;
+      if (r < N) {
+        zv[k] = zl ? z[r] + zl[r] : z[r];
+        yv[k] = ym[r];
+      }
+    }
+    float acc = 0.f;   // this thread's rows in FP32; float64 across threads
+#pragma unroll
+    for (int k = 0; k < kEpiRows; ++k) {
+      const int64_t r = r0 + threadIdx.x + (int64_t)kEpiThreads * k;
+      if (r >= ldz) break;
+      if (r >= N) {   // padding rows: zero residual, no likelihood term
+        Rhi[(size_t)c * ldz + r] = from_float<TO>(0.f);
+        if (Rlo) Rlo[(size_t)c * ldz + r] = from_float<TO>(0.f);
+        continue;
+      }
+      const float a = fabsf(zv[k]);
       const float e = tc::ex2_approx(a * kNegLog2eL);
       const float u = 1.f + e;
-      acc += (double)fmaf(kLn2L, tc::lg2_approx(u), 0.5f * a);
+      acc += fmaf(kLn2L, tc::lg2_approx(u), 0.5f * a);
       const float w = tc::rcp_approx(u) - 0.5f;
-      const float rv = zv >= 0.f ? ym[r] - w : ym[r] + w;
+      const float rv = zv[k] >= 0.f ? yv[k] - w : yv[k] + w;
       const TO h = from_float<TO>(rv);
       Rhi[(size_t)c * ldz + r] = h;
       if (Rlo) Rlo[(size_t)c * ldz + r] = from_float<TO>(rv - (float)h);
     }
-    acc = warp_sum(acc);
+    const double accd = warp_sum((double)acc);
     __syncthreads();                                   // red[] of the previous chain is read
-    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = accd;
     __syncthreads();
     if (threadIdx.x == 0) {
       double s = 0.0;
@@ -154,8 +181,9 @@ large_epilogue(const float* __restrict__ Z, const float* __restrict__ ym, int64_
 // One warp per chain: log-density from the partials (fixed order), the
 // linear term and the prior; gradient G - q / s^2.
 __global__ void large_finish(const double* __restrict__ part, int nblk, int n,
-                             const float* __restrict__ G, int ld, const float* __restrict__ q,
-                             int ldq, const double* __restrict__ lin, int D, float inv_var,
+                             const float* __restrict__ G, const float* __restrict__ Glo, int ld,
+                             const float* __restrict__ q, int ldq,
+                             const double* __restrict__ lin, int D, float inv_var,
                              double log_norm, double* __restrict__ logp,
                              float* __restrict__ grad, int ldg) {
   const int c = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
@@ -166,7 +194,8 @@ __global__ void large_finish(const double* __restrict__ part, int nblk, int n,
   for (int d = lane; d < D; d += 32) {
     const float qv = q[(size_t)c * ldq + d];
     t += lin[d] * (double)qv - 0.5 * (double)inv_var * (double)qv * (double)qv;
-    grad[(size_t)c * ldg + d] = G[(size_t)c * ld + d] - qv * inv_var;
+    const float g = Glo ? G[(size_t)c * ld + d] + Glo[(size_t)c * ld + d] : G[(size_t)c * ld + d];
+    grad[(size_t)c * ldg + d] = g - qv * inv_var;
   }
   t = warp_sum(t);
   if (lane == 0) logp[c] = t + (double)D * log_norm;
@@ -182,23 +211,23 @@ class LogregLarge final : public Target {
     ldz_ = (N_ + 7) / 8 * 8;
     xlo_ = mixed && x_dtype == 0;
     const size_t el = mixed ? 2 : 4;
-    xh_.reserve(el * (size_t)N_ * ld_);
-    if (xlo_) xl_.reserve(el * (size_t)N_ * ld_);
-    ym_.reserve(sizeof(float) * (size_t)N_);
-    const int64_t total = N_ * ld_;
+    xh_.reserve(el * (size_t)ldz_ * ld_);
+    if (xlo_) xl_.reserve(el * (size_t)ldz_ * ld_);
+    ym_.reserve(sizeof(float) * (size_t)ldz_);
+    const int64_t total = ldz_ * ld_;
     const unsigned blocks = (unsigned)((total + 255) / 256);
     cudaStream_t s = ctx->stream;
     if (mixed && x_dtype == 0)
       large_pack_kernel<float, __nv_bfloat16><<<blocks, 256, 0, s>>>(
-          static_cast<const float*>(X), y, N_, (int)D_, ld_, xh_.as<__nv_bfloat16>(),
+          static_cast<const float*>(X), y, N_, ldz_, (int)D_, ld_, xh_.as<__nv_bfloat16>(),
           xl_.as<__nv_bfloat16>(), ym_.as<float>());
     else if (mixed)
       large_pack_kernel<__nv_bfloat16, __nv_bfloat16><<<blocks, 256, 0, s>>>(
-          static_cast<const __nv_bfloat16*>(X), y, N_, (int)D_, ld_, xh_.as<__nv_bfloat16>(),
-          nullptr, ym_.as<float>());
+          static_cast<const __nv_bfloat16*>(X), y, N_, ldz_, (int)D_, ld_,
+          xh_.as<__nv_bfloat16>(), nullptr, ym_.as<float>());
     else
       large_pack_kernel<float, float><<<blocks, 256, 0, s>>>(
-          static_cast<const float*>(X), y, N_, (int)D_, ld_, xh_.as<float>(), nullptr,
+          static_cast<const float*>(X), y, N_, ldz_, (int)D_, ld_, xh_.as<float>(), nullptr,
           ym_.as<float>());
     GBM_CUDA(cudaGetLastError());
     {
@@ -222,81 +251,84 @@ class LogregLarge final : public Target {
     log_norm_ = -log((double)prior_scale) - 0.5 * log(2.0 * M_PI);
   }
 
-  // [B_hi | B_lo | Z | R_hi | R_lo | G | partials | cuBLAS workspace]
+  // Column sets: the mixed form stacks the hi and lo state (and residual)
+  // splits side by side, so each contraction is one GEMM of 2n columns whose
+  // halves are added in FP32 by the epilogue (Z) and the finish (G).
+  int sets() const { return mixed_ ? 2 : 1; }
+
+  // [B (sets x n rows) | Z (Np x sets n) | R | G (ld x sets n) | partials |
+  //  cuBLAS workspace]
   size_t workspace_bytes(int64_t cap) const override {
-    const size_t el = mixed_ ? 2 : 4;
+    const size_t el = mixed_ ? 2 : 4, w = (size_t)sets() * cap;
     const size_t nblk = (size_t)((N_ + kRowBlock - 1) / kRowBlock);
-    return align256(el * cap * ld_) * 2 + align256(4 * (size_t)ldz_ * cap) +
-           align256(el * (size_t)ldz_ * cap) * 2 + align256(4 * (size_t)cap * ld_) +
-           align256(8 * nblk * cap) + kCublasWs;
+    return align256(el * w * ld_) + align256(4 * (size_t)ldz_ * w) +
+           align256(el * (size_t)ldz_ * w) + align256(4 * w * ld_) + align256(8 * nblk * cap) +
+           kCublasWs;
   }
 
   void eval(const float* q, int ldq, const int*, int cap, double* logp, float* grad, int ldg,
             void* ws, cudaStream_t s) override {
     const size_t el = mixed_ ? 2 : 4;
     const int64_t nblk = (N_ + kRowBlock - 1) / kRowBlock;
+    const int n = cap, w = sets() * cap, D = (int)D_;
     unsigned char* p = static_cast<unsigned char*>(ws);
-    void* bhi = p;                 p += align256(el * cap * ld_);
-    void* blo = p;                 p += align256(el * cap * ld_);
-    float* Z = reinterpret_cast<float*>(p);    p += align256(4 * (size_t)ldz_ * cap);
-    void* rhi = p;                 p += align256(el * (size_t)ldz_ * cap);
-    void* rlo = p;                 p += align256(el * (size_t)ldz_ * cap);
-    float* G = reinterpret_cast<float*>(p);    p += align256(4 * (size_t)cap * ld_);
+    unsigned char* B = p;          p += align256(el * (size_t)w * ld_);
+    float* Z = reinterpret_cast<float*>(p);    p += align256(4 * (size_t)ldz_ * w);
+    unsigned char* R = p;          p += align256(el * (size_t)ldz_ * w);
+    float* G = reinterpret_cast<float*>(p);    p += align256(4 * (size_t)w * ld_);
     double* part = reinterpret_cast<double*>(p); p += align256(8 * (size_t)nblk * cap);
     void* cws = p;
     cublasHandle_t h = thread_handle(device_);
     GBM_CUBLAS(cublasSetStream(h, s));
     GBM_CUBLAS(cublasSetWorkspace(h, cws, kCublasWs));
-    const int N = (int)N_, D = (int)D_, n = cap;
     const unsigned sb = (unsigned)(((int64_t)n * ld_ + 255) / 256);
     if (mixed_)
       large_split_states<__nv_bfloat16><<<sb, 256, 0, s>>>(
-          q, ldq, n, D, ld_, static_cast<__nv_bfloat16*>(bhi), static_cast<__nv_bfloat16*>(blo));
+          q, ldq, n, D, ld_, reinterpret_cast<__nv_bfloat16*>(B),
+          reinterpret_cast<__nv_bfloat16*>(B) + (size_t)n * ld_);
     else
-      large_split_states<float><<<sb, 256, 0, s>>>(q, ldq, n, D, ld_, static_cast<float*>(bhi),
-                                                   nullptr);
+      large_split_states<float><<<sb, 256, 0, s>>>(q, ldq, n, D, ld_,
+                                                   reinterpret_cast<float*>(B), nullptr);
     GBM_CUDA(cudaGetLastError());
     const cudaDataType_t dt = mixed_ ? CUDA_R_16BF : CUDA_R_32F;
     const float one = 1.f, zero = 0.f;
-    // Z = X_hi B_hi^T (+ X_hi B_lo^T + X_lo B_hi^T): column-major (N x n),
-    // leading dimension ldz_ (N rounded up to 8 rows) so every column starts
-    // 16-byte aligned; K runs over the ld_ zero-padded features (a multiple
-    // of 8; the padding of X and of B is zero, so the sums are unchanged).
+    // Z = X_hi [B_hi; B_lo]^T (+ X_lo B_hi^T into the first n columns):
+    // column-major (Np x w) over the rows padded to a multiple of 8 and the
+    // ld_ zero-padded features: every extent the GEMMs see is a multiple of 8
+    // elements, so the library picks its aligned tensor-core kernels (with an
+    // odd row count it falls back to element-aligned ones, ~15x slower here);
+    // the padding of X and of B is zero, so the sums are unchanged.
     const int Kp = ld_, ldz = (int)ldz_;
-    auto gemm_z = [&](const void* xa, const void* bb, const float* beta) {
-      GBM_CUBLAS(cublasGemmEx(h, CUBLAS_OP_T, CUBLAS_OP_N, N, n, Kp, &one, xa, dt, ld_, bb, dt,
-                              ld_, beta, Z, CUDA_R_32F, ldz, CUBLAS_COMPUTE_32F,
+    auto gemm_z = [&](const void* xa, int cols, const float* beta) {
+      GBM_CUBLAS(cublasGemmEx(h, CUBLAS_OP_T, CUBLAS_OP_N, ldz, cols, Kp, &one, xa, dt, ld_, B,
+                              dt, ld_, beta, Z, CUDA_R_32F, ldz, CUBLAS_COMPUTE_32F,
                               CUBLAS_GEMM_DEFAULT));
     };
-    gemm_z(xh_.ptr, bhi, &zero);
-    if (mixed_) {
-      gemm_z(xh_.ptr, blo, &one);
-      if (xlo_) gemm_z(xl_.ptr, bhi, &one);
-    }
+    gemm_z(xh_.ptr, w, &zero);
+    if (xlo_) gemm_z(xl_.ptr, n, &one);
+    const float* Zlo = mixed_ ? Z + (size_t)n * ldz_ : nullptr;
     const dim3 eg((unsigned)nblk, (unsigned)std::min(n, 65535));
     if (mixed_)
-      large_epilogue<__nv_bfloat16><<<eg, 256, 0, s>>>(
-          Z, ym_.as<float>(), N_, ldz_, n, static_cast<__nv_bfloat16*>(rhi),
-          static_cast<__nv_bfloat16*>(rlo), part);
+      large_epilogue<__nv_bfloat16><<<eg, kEpiThreads, 0, s>>>(
+          Z, Zlo, ym_.as<float>(), N_, ldz_, n, reinterpret_cast<__nv_bfloat16*>(R),
+          reinterpret_cast<__nv_bfloat16*>(R) + (size_t)n * ldz_, part);
     else
-      large_epilogue<float><<<eg, 256, 0, s>>>(Z, ym_.as<float>(), N_, ldz_, n,
-                                               static_cast<float*>(rhi), nullptr, part);
+      large_epilogue<float><<<eg, kEpiThreads, 0, s>>>(Z, nullptr, ym_.as<float>(), N_, ldz_, n,
+                                               reinterpret_cast<float*>(R), nullptr, part);
     GBM_CUDA(cudaGetLastError());
-    // G^T = X_hi^T R_hi (+ X_hi^T R_lo + X_lo^T R_hi): column-major (ld x n)
-    // over all ld_ padded features (rows >= D come out zero and are not read).
-    auto gemm_g = [&](const void* xa, const void* rr, const float* beta) {
-      GBM_CUBLAS(cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, Kp, n, N, &one, xa, dt, ld_, rr, dt,
-                              ldz, beta, G, CUDA_R_32F, ld_, CUBLAS_COMPUTE_32F,
+    // G^T = X_hi^T [R_hi | R_lo] (+ X_lo^T R_hi into the first n columns):
+    // column-major (ld x w) over all ld_ padded features (rows >= D come out
+    // zero and are not read) and the Np padded rows (zero residuals).
+    auto gemm_g = [&](const void* xa, int cols, const float* beta) {
+      GBM_CUBLAS(cublasGemmEx(h, CUBLAS_OP_N, CUBLAS_OP_N, Kp, cols, ldz, &one, xa, dt, ld_, R,
+                              dt, ldz, beta, G, CUDA_R_32F, ld_, CUBLAS_COMPUTE_32F,
                               CUBLAS_GEMM_DEFAULT));
     };
-    gemm_g(xh_.ptr, rhi, &zero);
-    if (mixed_) {
-      gemm_g(xh_.ptr, rlo, &one);
-      if (xlo_) gemm_g(xl_.ptr, rhi, &one);
-    }
-    large_finish<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(part, (int)nblk, n, G, ld_, q, ldq,
-                                                        lin_.as<double>(), D, inv_var_,
-                                                        log_norm_, logp, grad, ldg);
+    gemm_g(xh_.ptr, w, &zero);
+    if (xlo_) gemm_g(xl_.ptr, n, &one);
+    large_finish<<<(unsigned)((n + 7) / 8), 256, 0, s>>>(
+        part, (int)nblk, n, G, mixed_ ? G + (size_t)n * ld_ : nullptr, ld_, q, ldq,
+        lin_.as<double>(), D, inv_var_, log_norm_, logp, grad, ldg);
     GBM_CUDA(cudaGetLastError());
   }
 

@@ -69,8 +69,8 @@ size_t estimate_bytes(const gbm_job_spec& s, int num_sms) {
     b += mixed ? N * Dp * 4.0 : N * (std::ceil(D / 16.0) * 16.0) * 4.0;
     b += N * 8.0;
     b += (2.0 * num_sms * 128.0 + C) * (8.0 + 4.0 * D);
-    if (D > (mixed ? 512.0 : 256.0))   // library-GEMM target: Z, R (hi + lo), G, cuBLAS
-      b += N * C * (mixed ? 8.0 : 12.0) + C * Dp * 12.0 + (32u << 20);
+    if (D > (mixed ? 512.0 : 256.0))   // library-GEMM target: Z and R (hi, lo), B, G, cuBLAS
+      b += (N + 8.0) * C * (mixed ? 12.0 : 8.0) + C * Dp * 16.0 + (32u << 20);
   } else if (s.family == GBM_FAMILY_MVN) {
     b += 4.0 * D * D + 4.0 * D + C * (8.0 * std::ceil(D / 64.0) + 4.0 * D);
   } else {
