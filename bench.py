@@ -405,6 +405,9 @@ def run_kernel_only(args, w):
   import probability_gb300 as pg
   if args.kernel_rows:   # a smaller case of the same shape (profiling)
     w = dict(w, n=args.kernel_rows)
+  if args.kernel_shape:   # rows,features,chains of another logistic posterior
+    n, d, c = (int(v) for v in args.kernel_shape.split(','))
+    w = dict(w, n=n, d=d, chains=c, feature_scale=d ** -0.5)
   X, y, init = make_data(w)
   target = pg.LogisticRegression(engine_features(X, w), y,
                                  precision=args.precision or w['precision'])
@@ -1563,6 +1566,9 @@ def main():
                   help='nuts_batch_256: transitions per chain at most in the free-running call')
   ap.add_argument('--kernel-rows', type=int, default=0,
                   help='with --kernel-only: rows of X (default: the workload\'s)')
+  ap.add_argument('--kernel-shape', default='',
+                  help='with --kernel-only: rows,features,chains (X drawn N(0, 1/features), '
+                       'stored in the workload\'s data type)')
   args = ap.parse_args()
   w = WORKLOADS[args.workload]
   if args.adapt:
