@@ -1272,7 +1272,7 @@ def run_batch(args, w):
   e2e = None
   if args.steps > 0:
     e2e_budget = min(budget, 2 * 1023)
-    e2e_k = 32
+    e2e_k = 256   # above what any chain completes in the budget
     h_q = q.cpu().pin_memory()
     h_l = kr.target_log_prob.cpu().pin_memory()
     h_g = kr.grads_target_log_prob.cpu().pin_memory()
@@ -1562,7 +1562,7 @@ def main():
                   help='nuts_batch_256: timed lock-step transitions beside the free-running call')
   ap.add_argument('--free-leaves', type=int, default=10230,
                   help='nuts_batch_256: leaf-iteration budget of the timed free-running call')
-  ap.add_argument('--free-transitions', type=int, default=256,
+  ap.add_argument('--free-transitions', type=int, default=512,
                   help='nuts_batch_256: transitions per chain at most in the free-running call')
   ap.add_argument('--kernel-rows', type=int, default=0,
                   help='with --kernel-only: rows of X (default: the workload\'s)')
