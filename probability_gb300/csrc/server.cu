@@ -1,13 +1,16 @@
 // Job server: many independent DA(NUTS) posteriors running concurrently.
 //
-// Each worker thread owns a context on a private non-blocking stream and
-// runs one job at a time to completion: build the target on its stream,
+// Each worker thread owns two contexts on private non-blocking streams (one
+// of the device's greatest priority, one of its least) and runs one job at a
+// time to completion on one of them: build the target on its stream,
 // evaluate the initial state, run the device-resident chain loop
-// (nuts_sample_chain) with dual averaging and the requested trace, copy the
-// final state out, free everything.  Buffers come from the stream-ordered
-// allocator (alloc_stream()), so a job's set-up and tear-down do not
-// synchronize the device and the other workers' kernels keep running.
-// Admission is first-in first-out under a device-memory budget.
+// (nuts_sample_chain: dual averaging, then the draws past its window
+// free-running) with the requested trace, copy the final state out, free
+// everything.  Jobs with little work per leaf take the high-priority stream.
+// Buffers come from the stream-ordered allocator (alloc_stream()), so a
+// job's set-up and tear-down do not synchronize the device and the other
+// workers' kernels keep running.  Admission is first-in first-out under a
+// device-memory budget.
 #include <cuda_runtime.h>
 
 #include <chrono>
