@@ -378,14 +378,17 @@ GBM_API int gbm_hmc_sample_chain(gbm_hmc* kernel, int64_t chains, float* state,
 /* ---- Job server: many independent posteriors at once ------------------- */
 
 /* There is no counterpart in the reference (it runs one sample_chain per
- * Python call).  A server owns `workers` host threads, each with its own
- * device stream.  Jobs -- one target family + DA(NUTS) sample_chain run --
- * are admitted first-in first-out while their estimated device memory fits
- * `memory_budget_bytes`; admitted jobs run concurrently on the workers'
- * streams with all chain and adaptation state resident on the device, and
- * their buffers come from the stream-ordered allocator so job set-up and
- * tear-down never synchronize the device.  Kernels are deterministic, so a
- * job's results do not depend on what else runs beside it. */
+ * Python call).  A server owns `workers` host threads, each with two device
+ * streams (the device's greatest and least priority; jobs with little work
+ * per leaf run on the first).  Jobs -- one target family + DA(NUTS)
+ * sample_chain run, the draws past the adaptation window free-running as
+ * with gbm_nuts_set_free_running -- are admitted first-in first-out while
+ * their estimated device memory fits `memory_budget_bytes`; admitted jobs
+ * run concurrently on the workers' streams with all chain and adaptation
+ * state resident on the device, and their buffers come from the
+ * stream-ordered allocator so job set-up and tear-down never synchronize
+ * the device.  Kernels are deterministic, so a job's results do not depend
+ * on what else runs beside it. */
 #define GBM_FAMILY_LOGISTIC_REGRESSION 0
 #define GBM_FAMILY_MVN 1
 #define GBM_FAMILY_HIERARCHICAL_NORMAL 2
