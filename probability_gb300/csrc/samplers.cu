@@ -275,7 +275,31 @@ __device__ void nuts_chain_leaf_pre(const NutsDev& w, int c, int j, int lane) {
   float* P = w.end_p[side];
   float* Q = w.end_q[side];
   const float* G = w.end_g[side];
-  for (int d = lane; d < D; d += 32) {
+  // Four elements per pass with every load issued before the stores (the
+  // arrays may alias as far as the compiler knows, so it would not hoist
+  // them itself); the arithmetic per element is the same as the tail's.
+  int d = lane;
+  for (; d + 96 < D; d += 128) {
+    float pv[4], gv[4], qv[4], iv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const size_t x = o + d + 32 * u;
+      pv[u] = P[x];
+      gv[u] = G[x];
+      qv[u] = Q[x];
+      iv[u] = imass(w, o, d + 32 * u);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const size_t x = o + d + 32 * u;
+      const float ph = pv[u] + he * gv[u];
+      const float qn = qv[u] + e * (ph * iv[u]);
+      P[x] = ph;
+      Q[x] = qn;
+      w.qw[oj + d + 32 * u] = qn;
+    }
+  }
+  for (; d < D; d += 32) {
     const float ph = P[o + d] + he * G[o + d];
     const float qn = Q[o + d] + e * (ph * imass(w, o, d));   // drift by the velocity
     P[o + d] = ph;
@@ -323,7 +347,35 @@ __device__ void nuts_chain_leaf_post(const NutsDev& w, int c, int j, int lane, u
   float* P = w.end_p[side];
   float* Gs = w.end_g[side];
   float kin_l = 0.f;
-  for (int d = lane; d < D; d += 32) {
+  // Four elements per pass, loads first (as in the half kick above); the
+  // tail loop is the per-element form.  kin_l accumulates in element order.
+  int d = lane;
+  for (; d + 96 < D; d += 128) {
+    float g2v[4], pv[4], csv[4], imv[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int x = d + 32 * u;
+      g2v[u] = w.gw[oj + x];
+      pv[u] = P[o + x];
+      csv[u] = w.cumsum[o + x];
+      imv[u] = imass(w, o, x);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int x = d + 32 * u;
+      const float p2 = (pv[u] + e * g2v[u]) - he * g2v[u];
+      P[o + x] = p2;
+      Gs[o + x] = g2v[u];
+      w.cumsum[o + x] = csv[u] + p2;
+      if (wslot >= 0) {
+        const size_t so = soff(w, c, wslot) + x;
+        w.slot_p[so] = p2 * imv[u];
+        w.slot_cs[so] = csv[u];
+      }
+      kin_l = fmaf(p2 * imv[u], p2, kin_l);
+    }
+  }
+  for (; d < D; d += 32) {
     const float g2 = w.gw[oj + d];
     const float p2 = (P[o + d] + e * g2) - he * g2;   // leapfrog_integrator.py:345-349,:304-309
     P[o + d] = p2;
