@@ -34,10 +34,11 @@ __host__ __device__ __forceinline__ int chunk_count(int n, int c_base, int c_lim
 
 // CTAs (or CTA pairs) of one launch: at most grid_max, and no more than the
 // call's chain tiles times the row splits that keep at least min_rows rows
-// each.  A small evaluation then occupies few SMs, so the launches of other
-// streams (other jobs) run beside it instead of waiting for a whole-GPU grid.
-// Kernels and the split reduction derive the split count from the grid they
-// are given, so passing this value to both keeps them consistent.
+// each, so no CTA is launched only to find no work.  With min_rows = 64 (the
+// smallest row tile) the split counts are those of the full grid: a small,
+// latency-bound evaluation keeps one row tile per CTA.  Kernels and the split
+// reduction derive the split count from the grid they are given, so passing
+// this value to both keeps them consistent.
 inline int work_grid(int grid_max, int64_t chains, int ct, int64_t N, int64_t min_rows) {
   const int64_t tiles = (chains + ct - 1) / ct;
   const int64_t s_cap = N / min_rows > 1 ? N / min_rows : 1;
@@ -46,7 +47,7 @@ inline int work_grid(int grid_max, int64_t chains, int ct, int64_t N, int64_t mi
   return g < 1 ? 1 : (int)g;
 }
 
-constexpr int64_t kMinSplitRows = 256;
+constexpr int64_t kMinSplitRows = 64;
 
 namespace {
 
