@@ -148,6 +148,39 @@ def test_nuts_reproducible_and_seed_dependent():
   assert not np.array_equal(a.next_state, c.next_state)
 
 
+def test_nuts_chain_transitions_do_not_depend_on_the_batch():
+  """The lock-step NUTS transition (nuts.py:541-711: finished chains only
+  idle under the batch's masks) gives every chain the transition it would
+  have alone with the same draws -- the property free-running NUTS uses to
+  let each chain start its next transition on its own.  A batch of 5 chains
+  over 3 transitions equals each chain run alone with its draws addressed
+  as part of the batch (OffsetDraws): the same trajectory lengths exactly,
+  states and log-densities to 1e-12 (NumPy's BLAS rounds a 5-row product
+  and a 1-row product differently, in the last bit)."""
+  rng = np.random.default_rng(3)
+  D, C = 4, 5
+  A = rng.normal(size=(D, D + 2)) / np.sqrt(D)
+  t = targets.MultivariateNormalTriL(rng.normal(size=D), np.linalg.cholesky(A @ A.T))
+  x = rng.normal(size=(C, D)) * 0.5
+  eps = np.array([0.2, 0.3, 0.25, 0.15, 0.35])
+  lp, g = t(x)
+  batch = [(x, lp, g)]
+  alone = [[(x[c:c + 1], lp[c:c + 1], g[c:c + 1])] for c in range(C)]
+  for step in range(3):
+    key = (11, step)
+    q, l, gr = batch[-1]
+    r = mcmc.nuts_one_step(t, q, l, gr, eps, philox.PhiloxDraws(key), 6)
+    batch.append((r.next_state, r.target_log_prob, r.grads_target_log_prob))
+    for c in range(C):
+      qc, lc, gc = alone[c][-1]
+      rc = mcmc.nuts_one_step(t, qc, lc, gc, eps[c:c + 1],
+                              philox.OffsetDraws(key, chain0=c, elem0=c * D), 6)
+      alone[c].append((rc.next_state, rc.target_log_prob, rc.grads_target_log_prob))
+      np.testing.assert_array_equal(rc.leapfrogs_taken[0], r.leapfrogs_taken[c])
+      np.testing.assert_allclose(rc.next_state[0], r.next_state[c], rtol=1e-12, atol=1e-12)
+      np.testing.assert_allclose(rc.target_log_prob[0], r.target_log_prob[c], rtol=1e-12)
+
+
 def test_leapfrog_energy_conservation():
   # leapfrog_integrator_test.py:48-73: 1000 steps, rtol 0.02 on energy.
   def tgt(x):
