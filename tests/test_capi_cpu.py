@@ -53,6 +53,14 @@ def test_host_only_entry_points(libpath):
   # Argument errors are reported, not crashed on.
   assert lib.gbm_nuts_create(None, 1, 10, 1000.0, 1, None) == _native.GBM_EINVAL
   assert b'NULL' in lib.gbm_last_error()
+  # The free-running entry points validate before touching a device.
+  assert lib.gbm_nuts_set_free_running(None, 1) == _native.GBM_EINVAL
+  assert b'NULL' in lib.gbm_last_error()
+  i64 = ctypes.c_int64()
+  assert lib.gbm_nuts_run_free(None, 8, None, None, None, None, 0, _native.seed_words((1, 2)),
+                               0, 4, 100, None, None, None, None, None, None, None,
+                               ctypes.byref(i64)) == _native.GBM_EINVAL
+  assert b'NULL' in lib.gbm_last_error()
 
 
 def test_python_instruction_tables_match_reference(golden_dir):
